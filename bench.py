@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Benchmark of the RB-ThermoParticles hot path on GB300: MLUPS and %HBM roofline.
+
+Workload (headline): 320x320x160 single-phase Rayleigh-Benard, Ra=1e8, Pr=0.71, D3Q27 f+g, seeded
+linear-conduction start, populations stored in FP32 (FP32 arithmetic).  The same workload is also
+timed with FP64 storage/arithmetic (the parity path) and shifted-FP16 storage, and the
+particle-laden variant (1000 spheres of diameter 16) with FP64 and FP32 storage; those appear as
+sub-objects of the one JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one full time step of the whole lattice (16.384 M nodes).  `value` = MLUPS with the state
+resident in HBM, timed with CUDA events on the library's stream; the populations (7.3 GB at FP32)
+exceed L2, so no flush is needed between steps.  `e2e` runs the same K steps through the public C
+ABI starting from host (numpy) buffers: the state upload and the Nu / mean-field read-back are
+inside the timed region.  `--impl reference` times the CPU oracle (the restated reference step,
+OpenMP FP64) on a bounded slab of the same workload with all host threads.
+
+Multi-GPU: the path does not shard (one cavity per GPU); N>1 runs N independent replicas, takes
+the max time over ranks and reports the aggregate ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "rb-thermoparticles_gb300"))
+
+MEASURED_PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def bytes_per_node(storage: int) -> int:
+    """Algorithmic HBM bytes per lattice-node update: read+write 27 f and 27 g populations plus
+    read+write of the FP64 buoyancy auxiliary F_x."""
+    s = {0: 8, 1: 4, 2: 2}[storage]
+    return 2 * 54 * s + 2 * 8
+
+
+def hbm_peak():
+    try:
+        with open(MEASURED_PEAKS) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ----------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ----------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join(REPO, "gpurun_out" if os.path.isdir(os.path.join(REPO, "gpurun_out")) else "_work",
+                                 f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        try:
+            for line in open(self.path):
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9 and p[1].isdigit():
+                    rows.append(p)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [int(r[1]) for r in rows]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": int(rows[0][2]), "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------------------------
+def _events(torch, solver):
+    import ctypes
+    ptr = ctypes.c_void_p()
+    solver.lib.rbtp_get_stream(solver.handle, ctypes.byref(ptr))
+    stream = torch.cuda.ExternalStream(ptr.value)
+    return stream, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def time_variant(torch, name, storage, steps, warmup, dist=None, keep_state=False):
+    """Device-timed MLUPS of one variant with the state resident in HBM."""
+    from rbtp import Solver, workloads as W
+    cfg = W.config(name, storage=storage)
+    s = Solver(cfg)
+    f, g, f7 = W.initial_state(cfg)
+    if cfg.activate_particles:
+        s.initialize()          # seeded sphere placement (pinit.cu:97-144)
+        s.load_state(f, g, f7, s.particles())
+    else:
+        s.load_state(f, g, f7)
+    del f, g, f7
+    s.step(warmup)
+    stream, e0, e1 = _events(torch, s)
+    _barrier(dist)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    s.step(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    ms = _max_over_ranks(torch, dist, ms)
+    L = cfg.nodes
+    out = {"workload": name, "storage": ["f64", "f32", "f16s"][storage], "ms_per_step": ms / steps,
+           "mlups": L * steps / (ms * 1e-3) / 1e6, "nodes": L,
+           "launches_per_step": 1 if not cfg.activate_particles else 14}
+    if cfg.activate_particles:
+        out["npart"] = s.npart
+    if keep_state:
+        return out, s
+    s.close()
+    return out
+
+
+def e2e_variant(torch, name, storage, steps, dist=None):
+    """Same metric through the public API from host buffers: state upload, K steps, Nu + means
+    read-back, all inside the timed region."""
+    import numpy as np
+    from rbtp import Solver, workloads as W
+    cfg = W.config(name, storage=storage)
+    s = Solver(cfg)
+    f, g, f7 = W.initial_state(cfg)
+    s.load_state(f, g, f7)          # warm the allocation and the load path once
+    s.step(2)
+    _barrier(dist)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.load_state(f, g, f7)
+    s.step(steps, macros_last=True)
+    row = s.nu(s.istep)
+    means = s.means()
+    t1 = time.perf_counter()
+    sec = _max_over_ranks(torch, dist, (t1 - t0) * 1e3) * 1e-3
+    assert np.all(np.isfinite(row)) and np.all(np.isfinite(means))
+    h2d = f.nbytes + g.nbytes + f7.nbytes
+    d2h = 7 * 8 + 4 * 8 + 10 * 8 * cfg.lx  # Nu row, means, per-plane sums
+    s.close()
+    return {"value": cfg.nodes * steps / sec / 1e6, "unit": "MLUPS",
+            "h2d_bytes_per_step": h2d / steps, "d2h_bytes_per_step": d2h / steps,
+            "seconds": sec, "includes": "state upload from host + K steps + Nu/means read-back"}
+
+
+def cpu_baseline(steps: int = 3, nz: int = 40):
+    """The oracle (FP64 OpenMP restatement of the reference step) on a slab of the production
+    grid, all host threads."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py
+    from rbtp import workloads as W
+    threads = oracle_py.set_threads(os.cpu_count() or 1)
+    cfg = W.config("production", lz=nz)
+    o = oracle_py.Oracle(cfg)
+    f, g, f7 = W.initial_state(cfg)
+    o.load_state(f, g, f7)
+    del f, g, f7
+    o.step(1)
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": cfg.nodes * steps / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{cfg.lx}x{cfg.ly}x{cfg.lz} slab of the 320x320x160 single-phase workload, "
+                      f"{steps} steps, FP64 oracle"}
+
+
+def _barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def _max_over_ranks(torch, dist, v):
+    if dist is None:
+        return v
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_ours(args) -> dict:
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+        dist = td
+    else:
+        torch.cuda.set_device(0)
+    import rbtp_build
+    if rank == 0 or world == 1:
+        rbtp_build.build(host=False)
+    _barrier(dist)
+    peak, peak_src = hbm_peak()
+
+    # headline: FP32 storage, clocks sampled over its timed region
+    with ClockSampler(local) as clk:
+        head = time_variant(torch, "production", 1, args.steps, args.warmup, dist)
+    clocks = clk.summary()
+    fp64 = time_variant(torch, "production", 0, args.steps, args.warmup, dist)
+    f16 = time_variant(torch, "production", 2, args.steps, args.warmup, dist)
+    psteps = max(3, min(args.steps, 20))
+    p64 = time_variant(torch, "particle_laden", 0, psteps, args.warmup, dist)
+    p32 = time_variant(torch, "particle_laden", 1, psteps, args.warmup, dist)
+    e2e = e2e_variant(torch, "production", 1, args.steps, dist)
+
+    def roof(v):
+        b = bytes_per_node(["f64", "f32", "f16s"].index(v["storage"]))
+        achieved = v["nodes"] * b / (v["ms_per_step"] * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                "bytes_per_node": b, "traffic": None}
+
+    for v in (head, fp64, f16, p64, p32):
+        v["roofline"] = roof(v)
+    value = head["mlups"] * world
+    line = {
+        "metric": "MLUPS (lattice-node updates/s), 320x320x160 D3Q27 f+g RB step, FP32-store",
+        "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(head["ms_per_step"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded linear-conduction start (SplitMix64 +-1e-3 perturbation)",
+        "config": {"workload": "production single-phase RB 320x320x160, Ra=1e8, Pr=0.71, FP32-store",
+                   "nodes": head["nodes"], "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "l2": "state (7.3 GB) exceeds L2; no flush needed"},
+        "roofline": head["roofline"],
+        "clocks": clocks,
+        "gpu_launches": head["launches_per_step"] * args.steps,
+        "e2e": e2e,
+        "fp64": fp64, "fp16s": f16, "particle_laden_fp64": p64, "particle_laden_fp32": p32,
+        "fp32_over_fp64": round(head["mlups"] / fp64["mlups"], 3),
+    }
+    if rank == 0:
+        try:
+            line["cpu_baseline"] = cpu_baseline()
+        except Exception as exc:  # reported, not fatal
+            line["cpu_baseline"] = {"value": None, "error": str(exc)}
+    if dist is not None:
+        dist.destroy_process_group()
+    return line if rank == 0 else None
+
+
+def run_reference(args) -> dict | None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle_py
+    from rbtp import workloads as W
+    threads = oracle_py.set_threads(os.cpu_count() or 1)
+    nz = 16
+    cfg = W.config("production", lz=nz)
+    o = oracle_py.Oracle(cfg)
+    f, g, f7 = W.initial_state(cfg)
+    o.load_state(f, g, f7)
+    del f, g, f7
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    v = cfg.nodes * args.steps / dt / 1e6
+    sample = (f"{cfg.lx}x{cfg.ly}x{nz} slab of the 320x320x160 workload per step, "
+              f"FP64 oracle (OpenMP restatement of the reference CUDA step)")
+    return {"metric": "MLUPS (lattice-node updates/s), 320x320x160 D3Q27 f+g RB step, FP32-store",
+            "value": round(v, 3), "unit": "MLUPS", "impl": "reference", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "production single-phase RB 320x320x160, Ra=1e8, Pr=0.71 (slab sample)"},
+            "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

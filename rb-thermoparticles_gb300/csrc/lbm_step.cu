@@ -1,0 +1,419 @@
+// lbm_step.cu — fused D3Q27 f+g pull-stream / collide kernel for sm_103a.
+//
+// One thread per lattice node.  The kernel replaces the reference's per-step sequence
+//   macrovar (macrovar.cu:3-34) -> forcing (macrovar.cu:36-47) -> collision_BGK (collision.cu:3-33)
+//   -> f_collide copy -> streaming (streaming.cu:3-23) -> collision_BGK_scalar (collision.cu:35-89)
+//   -> g_collide copy -> streaming_scalar (streaming.cu:25-63)
+// with a single read and a single write of every population.  The streaming of step n is
+// performed by the pull at the start of step n+1: the buffer written by step n holds the
+// post-collision populations f*(n) at their home node, and node x gathers f_i(x) = f*_i(x - c_i)
+// (or the wall bounce-back/Dirichlet image when x - c_i is outside the box).  Sparse particle
+// corrections (IBB, refill) are written by their own kernels into exactly the slots this gather
+// reads, so the bulk kernel never branches on solid flags.
+//
+// The collision is the reference's BGK algebra regrouped by direction pairs (i, opp(i)): with
+// A = 4.5 (c.u)^2 - 1.5 u^2 (even in c) and B = 3 c.u (odd in c), both f and g post-collision
+// values split into a pair-symmetric and a pair-antisymmetric part.  The g source term of
+// collision.cu:57-88 reduces to w_i c_i.V with one per-node vector V because it is linear in c_i;
+// its first pass (the non-equilibrium first moment) is sum_i c_i g_i - phi u exactly.
+#include "rbtp_internal.cuh"
+
+namespace rbtp {
+
+namespace {
+
+struct NodeIdx {
+    int ix, iy, iz;
+    long long node;
+};
+
+template <int MODE, bool PULL, int OUT>
+__global__ void __launch_bounds__(128) k_step(const Geo geo, const Phys ph, const StepBuffers b)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    using R = typename ST::R;
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    const int iz = blockIdx.z;
+    if (ix >= geo.lx || iy >= geo.ly) return;
+    const long long L = geo.L;
+    const long long node = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
+    const S *__restrict__ fin = static_cast<const S *>(b.fin);
+    const S *__restrict__ gin = static_cast<const S *>(b.gin);
+    S *__restrict__ fout = static_cast<S *>(b.fout);
+    S *__restrict__ gout = static_cast<S *>(b.gout);
+    const double t0 = ph.t0;
+
+    const bool xlo = ix == 0, xhi = ix == geo.lx - 1;
+    const bool ylo = iy == 0, yhi = iy == geo.ly - 1;
+    const bool zlo = iz == 0, zhi = iz == geo.lz - 1;
+    const long long wall_slot = (long long)iz * geo.ly + iy;
+    double rw = 0.0;
+    if (PULL && (xlo || xhi)) rw = b.rho_wall[(xhi ? (long long)geo.lz * geo.ly : 0) + wall_slot];
+
+    R f[27], g[27];
+    unroll<27>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i), o = dopp(i);
+        constexpr double w = dweight(i);
+        if constexpr (!PULL || i == 0) {
+            f[i] = ST::ld_f(fin + (long long)i * L + node, w, t0);
+            g[i] = ST::ld_g(gin + (long long)i * L + node, w, t0);
+        } else {
+            const bool ox = (cx == 1 && xlo) || (cx == -1 && xhi);
+            const bool oy = (cy == 1 && ylo) || (cy == -1 && yhi);
+            const bool oz = (cz == 1 && zlo) || (cz == -1 && zhi);
+            const bool out = ox || oy || oz;
+            const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
+            const long long src = out ? ((long long)o * L + node) : ((long long)i * L + node - off);
+            f[i] = ST::ld_f(fin + src, w, t0);
+            R gr = ST::ld_g(gin + src, w, t0);
+            // streaming.cu:45-61: a z or y exit is adiabatic even at the x walls; only a pure
+            // x exit takes the Dirichlet anti-bounce-back with the node's density deviation.
+            if (ox && !oy && !oz) {
+                const double tw = (cx == 1) ? ph.thot : ph.tcold;
+                gr = (R)(-(double)gr + 2.0 * w * tw * (1.0 + rw));
+            }
+            g[i] = gr;
+        }
+    });
+
+    // ---- moments (macrovar.cu:3-34), pairwise ----
+    R rho = f[0], jx = 0, jy = 0, jz = 0;
+    R phi = g[0], kx = 0, ky = 0, kz = 0;
+    unroll<13>([&](auto K) {
+        constexpr int i = dpair(decltype(K)::value);
+        constexpr int o = dopp(i);
+        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+        const R sf = f[i] + f[o], df = f[i] - f[o];
+        const R sg = g[i] + g[o], dg = g[i] - g[o];
+        rho += sf;
+        phi += sg;
+        if constexpr (cx == 1) { jx += df; kx += dg; }
+        if constexpr (cx == -1) { jx -= df; kx -= dg; }
+        if constexpr (cy == 1) { jy += df; ky += dg; }
+        if constexpr (cy == -1) { jy -= df; ky -= dg; }
+        if constexpr (cz == 1) { jz += df; kz += dg; }
+        if constexpr (cz == -1) { jz -= df; kz -= dg; }
+    });
+    if (!(fabs((double)rho) < 1e30) || !(fabs((double)phi) < 1e30)) atomicOr(&b.status->nonfinite, 1);
+
+    const double fold = b.faux[node];
+    const R ux = jx + (R)(0.5 * fold), uy = jy, uz = jz;
+    // forcing (macrovar.cu:45): F_x = g0 beta (phi - T0); F_y = F_z = 0 always
+    const R Fx = (R)(ph.grav0 * ph.beta) * (phi - (R)t0);
+    b.faux[node] = (double)Fx;
+
+    if constexpr (OUT >= OUT_MACROS) {
+        b.rho[node] = (double)rho;
+        b.ux[node] = (double)ux;
+        b.uy[node] = (double)uy;
+        b.uz[node] = (double)uz;
+        b.phi[node] = (double)phi;
+    } else if constexpr (OUT == OUT_RHO) {
+        b.rho[node] = (double)rho;
+    }
+    if (xlo) b.rho_wall[wall_slot] = (double)rho;
+    if (xhi) b.rho_wall[(long long)geo.lz * geo.ly + wall_slot] = (double)rho;
+
+    // ---- f collision (collision.cu:3-33) ----
+    const R tinv = (R)(1.0 / ph.tau);
+    const R om = (R)(1.0 - 1.0 / ph.tau);
+    const R G = (R)(3.0 * (1.0 - 0.5 / ph.tau)) * Fx;
+    const R Gux = G * ux;
+    const R h = (R)1.5 * (ux * ux + uy * uy + uz * uz);
+    const R k1 = tinv - Gux;
+    const R k0 = rho * tinv - Gux;
+    // ---- g collision (collision.cu:35-89) ----
+    const R tcinv = (R)(1.0 / ph.tauc);
+    const R omc = (R)(1.0 - 1.0 / ph.tauc);
+    const R gd = rho / (R)3 + (R)(2.0 * ph.tauc / 3.0);
+    const R rgd = rho / gd;
+    const R Rc = (R)(1.0 - 1.0 / (2.0 * ph.tauc));
+    const R c2 = (R)(-2) * rgd * Rc;
+    const R Vx = c2 * (kx - phi * ux) + Rc * Fx * phi * ((R)3 - rgd);
+    const R Vy = c2 * (ky - phi * uy);
+    const R Vz = c2 * (kz - phi * uz);
+    const R pt = phi * tcinv;
+    const R ptb = pt * ((R)1 + rho);
+
+    {
+        constexpr R w0 = (R)dweight(0);
+        f[0] = om * f[0] + w0 * (k0 - h * k1);
+        g[0] = omc * g[0] + (w0 * (ptb - pt * h) - pt * rho);
+    }
+    unroll<13>([&](auto K) {
+        constexpr int i = dpair(decltype(K)::value);
+        constexpr int o = dopp(i);
+        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+        constexpr R w = (R)dweight(i);
+        R cu = 0, cV = 0;
+        if constexpr (cx != 0) { cu += (R)cx * ux; cV += (R)cx * Vx; }
+        if constexpr (cy != 0) { cu += (R)cy * uy; cV += (R)cy * Vy; }
+        if constexpr (cz != 0) { cu += (R)cz * uz; cV += (R)cz * Vz; }
+        const R A = (R)4.5 * cu * cu - h;
+        const R B = (R)3 * cu;
+        R fS = A * k1 + k0;
+        R fD = B * k1;
+        if constexpr (cx != 0) {
+            fS += (R)cx * (G * B);
+            fD += (R)cx * (G + G * A);
+        }
+        const R gS = A * pt + ptb;
+        const R gD = B * pt + cV;
+        const R fi = f[i], fo = f[o], gi = g[i], go = g[o];
+        f[i] = om * fi + w * (fS + fD);
+        f[o] = om * fo + w * (fS - fD);
+        g[i] = omc * gi + w * (gS + gD);
+        g[o] = omc * go + w * (gS - gD);
+    });
+
+    unroll<27>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        constexpr double w = dweight(i);
+        ST::st_f(fout + (long long)i * L + node, f[i], w, t0);
+        ST::st_g(gout + (long long)i * L + node, g[i], w, t0);
+        if constexpr (OUT == OUT_MACROS_COL) {
+            b.fcol[(long long)i * L + node] = (double)f[i];
+            b.gcol[(long long)i * L + node] = (double)g[i];
+        }
+    });
+}
+
+// Stream-only export: the post-streaming populations f(n) of the reference (its d_f / d_g after a
+// step) reconstructed from the post-collision buffer, as FP64 home layout.
+template <int MODE>
+__global__ void __launch_bounds__(128) k_stream_export(const Geo geo, const Phys ph, const void *fin_,
+                                                       const void *gin_, const double *rho_wall,
+                                                       double *fout, double *gout)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+    const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+    const int iz = blockIdx.z;
+    if (ix >= geo.lx || iy >= geo.ly) return;
+    const long long L = geo.L;
+    const long long node = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
+    const S *fin = static_cast<const S *>(fin_);
+    const S *gin = static_cast<const S *>(gin_);
+    const bool xlo = ix == 0, xhi = ix == geo.lx - 1;
+    const bool ylo = iy == 0, yhi = iy == geo.ly - 1;
+    const bool zlo = iz == 0, zhi = iz == geo.lz - 1;
+    const long long wall_slot = (long long)iz * geo.ly + iy;
+    double rw = 0.0;
+    if (xlo || xhi) rw = rho_wall[(xhi ? (long long)geo.lz * geo.ly : 0) + wall_slot];
+    unroll<27>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i), o = dopp(i);
+        constexpr double w = dweight(i);
+        const bool ox = (cx == 1 && xlo) || (cx == -1 && xhi);
+        const bool oy = (cy == 1 && ylo) || (cy == -1 && yhi);
+        const bool oz = (cz == 1 && zlo) || (cz == -1 && zhi);
+        const bool out = ox || oy || oz;
+        const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
+        const long long src = out ? ((long long)o * L + node) : ((long long)i * L + node - off);
+        fout[(long long)i * L + node] = (double)ST::ld_f(fin + src, w, ph.t0);
+        double gr = (double)ST::ld_g(gin + src, w, ph.t0);
+        if (ox && !oy && !oz) {
+            const double tw = (cx == 1) ? ph.thot : ph.tcold;
+            gr = -gr + 2.0 * w * tw * (1.0 + rw);
+        }
+        gout[(long long)i * L + node] = gr;
+    });
+}
+
+template <int MODE>
+__global__ void k_home_export(const Geo geo, const Phys ph, const void *fin_, const void *gin_,
+                              double *fout, double *gout)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= geo.L) return;
+    const S *fin = static_cast<const S *>(fin_);
+    const S *gin = static_cast<const S *>(gin_);
+    unroll<27>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        constexpr double w = dweight(i);
+        fout[(long long)i * geo.L + n] = (double)ST::ld_f(fin + (long long)i * geo.L + n, w, ph.t0);
+        gout[(long long)i * geo.L + n] = (double)ST::ld_g(gin + (long long)i * geo.L + n, w, ph.t0);
+    });
+}
+
+template <int MODE>
+__global__ void k_home_import(const Geo geo, const Phys ph, const double *fin, const double *gin,
+                              void *fout_, void *gout_)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    using R = typename ST::R;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= geo.L) return;
+    S *fout = static_cast<S *>(fout_);
+    S *gout = static_cast<S *>(gout_);
+    unroll<27>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        constexpr double w = dweight(i);
+        ST::st_f(fout + (long long)i * geo.L + n, (R)fin[(long long)i * geo.L + n], w, ph.t0);
+        ST::st_g(gout + (long long)i * geo.L + n, (R)gin[(long long)i * geo.L + n], w, ph.t0);
+    });
+}
+
+// init_f / init_g (initial.cu:335-397): deviation-form rest f = 0; g from the equilibrium at
+// T = T_REF with the rho field that init_f set to RHO0.
+template <int MODE>
+__global__ void k_fresh_init(const Geo geo, const Phys ph, void *f_, void *g_, double *faux,
+                             double *rho, double *ux, double *uy, double *uz, double *phi)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    using R = typename ST::R;
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= geo.L) return;
+    S *f = static_cast<S *>(f_);
+    S *g = static_cast<S *>(g_);
+    const double r = ph.rho0;
+    const double tT = ph.t0;
+    const double lambda0 = 1.0 - dweight(0);
+    rho[n] = ph.rho0;
+    ux[n] = 0.0; uy[n] = 0.0; uz[n] = 0.0;
+    phi[n] = tT;
+    faux[n] = ph.grav0 * ph.beta * (tT - ph.t0);
+    unroll<27>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        constexpr double w = dweight(i);
+        double geq = w * tT * (1.0 + 0.0 + 0.5 * (0.0 - 0.0));
+        if (i == 0) geq -= lambda0 * tT * r;
+        else geq += w * tT * r;
+        ST::st_f(f + (long long)i * geo.L + n, (R)(w * (0.0 + 0.0 + 0.5 * (0.0 - 0.0))), w, ph.t0);
+        ST::st_g(g + (long long)i * geo.L + n, (R)geq, w, ph.t0);
+    });
+}
+
+// macrovar (macrovar.cu:3-34) on FP64 home-layout arrays with zero force (restart without the
+// %09d.dat fields).
+__global__ void k_macros_from_home(const Geo geo, const double *f, const double *g, double *rho,
+                                   double *ux, double *uy, double *uz, double *phi)
+{
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= geo.L) return;
+    double r = 0, jx = 0, jy = 0, jz = 0, p = 0;
+    unroll<27>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        const double fv = f[(long long)i * geo.L + n];
+        r += fv;
+        jx += dcx(i) * fv;
+        jy += dcy(i) * fv;
+        jz += dcz(i) * fv;
+        p += g[(long long)i * geo.L + n];
+    });
+    rho[n] = r; ux[n] = jx; uy[n] = jy; uz[n] = jz; phi[n] = p;
+}
+
+__global__ void k_forcing(const Geo geo, const Phys ph, const double *phi, double *faux)
+{
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= geo.L) return;
+    faux[n] = ph.grav0 * ph.beta * (phi[n] - ph.t0);
+}
+
+inline dim3 node_grid(const Geo &g, dim3 blk)
+{
+    return dim3((g.lx + blk.x - 1) / blk.x, (g.ly + blk.y - 1) / blk.y, g.lz);
+}
+inline unsigned lin_blocks(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+template <int MODE>
+cudaError_t launch_step_mode(bool pull, int out, const Geo &geo, const Phys &ph,
+                             const StepBuffers &b, cudaStream_t st)
+{
+    const dim3 blk(32, 4, 1);
+    const dim3 grd = node_grid(geo, blk);
+#define RBTP_STEP_CASE(P, O)                                                       \
+    if (pull == P && out == O) {                                                   \
+        k_step<MODE, P, O><<<grd, blk, 0, st>>>(geo, ph, b);                       \
+        return cudaGetLastError();                                                 \
+    }
+    RBTP_STEP_CASE(true, OUT_NONE)
+    RBTP_STEP_CASE(true, OUT_RHO)
+    RBTP_STEP_CASE(true, OUT_MACROS)
+    RBTP_STEP_CASE(true, OUT_MACROS_COL)
+    RBTP_STEP_CASE(false, OUT_NONE)
+    RBTP_STEP_CASE(false, OUT_RHO)
+    RBTP_STEP_CASE(false, OUT_MACROS)
+    RBTP_STEP_CASE(false, OUT_MACROS_COL)
+#undef RBTP_STEP_CASE
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+cudaError_t launch_step(int mode, bool pull, int out, const Geo &geo, const Phys &ph,
+                        const StepBuffers &b, cudaStream_t st)
+{
+    switch (mode) {
+    case RBTP_STORE_F64: return launch_step_mode<RBTP_STORE_F64>(pull, out, geo, ph, b, st);
+    case RBTP_STORE_F32: return launch_step_mode<RBTP_STORE_F32>(pull, out, geo, ph, b, st);
+    case RBTP_STORE_F16S: return launch_step_mode<RBTP_STORE_F16S>(pull, out, geo, ph, b, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+#define RBTP_MODE_DISPATCH(mode, CALL)                                  \
+    switch (mode) {                                                     \
+    case RBTP_STORE_F64: { constexpr int M = RBTP_STORE_F64; CALL; break; } \
+    case RBTP_STORE_F32: { constexpr int M = RBTP_STORE_F32; CALL; break; } \
+    case RBTP_STORE_F16S: { constexpr int M = RBTP_STORE_F16S; CALL; break; } \
+    default: return cudaErrorInvalidValue;                              \
+    }
+
+cudaError_t launch_stream_export(int mode, const Geo &geo, const Phys &ph, const void *fin,
+                                 const void *gin, const double *rho_wall, double *fout,
+                                 double *gout, cudaStream_t st)
+{
+    const dim3 blk(32, 4, 1);
+    const dim3 grd = node_grid(geo, blk);
+    RBTP_MODE_DISPATCH(mode, (k_stream_export<M><<<grd, blk, 0, st>>>(geo, ph, fin, gin, rho_wall, fout, gout)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_home_export(int mode, const Geo &geo, const Phys &ph, const void *fin,
+                               const void *gin, double *fout, double *gout, cudaStream_t st)
+{
+    RBTP_MODE_DISPATCH(mode, (k_home_export<M><<<lin_blocks(geo.L, 256), 256, 0, st>>>(geo, ph, fin, gin, fout, gout)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_home_import(int mode, const Geo &geo, const Phys &ph, const double *fin,
+                               const double *gin, void *fout, void *gout, cudaStream_t st)
+{
+    RBTP_MODE_DISPATCH(mode, (k_home_import<M><<<lin_blocks(geo.L, 256), 256, 0, st>>>(geo, ph, fin, gin, fout, gout)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fresh_init(int mode, const Geo &geo, const Phys &ph, void *f, void *g,
+                              double *faux, double *rho, double *ux, double *uy, double *uz,
+                              double *phi, cudaStream_t st)
+{
+    RBTP_MODE_DISPATCH(mode, (k_fresh_init<M><<<lin_blocks(geo.L, 256), 256, 0, st>>>(geo, ph, f, g, faux, rho, ux, uy, uz, phi)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_macros_from_home(const Geo &geo, const double *f, const double *g, double *rho,
+                                    double *ux, double *uy, double *uz, double *phi,
+                                    cudaStream_t st)
+{
+    k_macros_from_home<<<lin_blocks(geo.L, 256), 256, 0, st>>>(geo, f, g, rho, ux, uy, uz, phi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_forcing(const Geo &geo, const Phys &ph, const double *phi, double *faux,
+                           cudaStream_t st)
+{
+    k_forcing<<<lin_blocks(geo.L, 256), 256, 0, st>>>(geo, ph, phi, faux);
+    return cudaGetLastError();
+}
+
+}  // namespace rbtp

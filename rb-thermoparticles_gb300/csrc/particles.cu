@@ -1,0 +1,827 @@
+// particles.cu — particle coupling kernels for sm_103a.
+//
+// Replaces src_part/{links,ibb,pforces,move,refill}.cu.  Design:
+//   * solid marking: one launch over all particles' bounding boxes; the lowest pid that contains a
+//     node owns it (atomicMin), which is the reference's "first serialized launch wins" rule
+//     (links.cu:45, 160-188) without N serialized launches or host round trips;
+//   * IBB links: a fixed-capacity slab per particle, filled by one CTA per particle in
+//     (node, direction) order, so the list is compact per particle and needs no global scan or
+//     host-side count (links.cu:50-139, 196-250);
+//   * IBB f/g, momentum exchange and heat flux: one CTA per particle walks its slab, writes the
+//     bounce-back values straight into the pull slots the next step reads, and reduces force,
+//     torque and heat with a fixed-order tree — deterministic, no floating-point atomics
+//     (ibb.cu:5-205);
+//   * contacts: a cell list; each particle sums its partners in ascending pid order, the order the
+//     reference's pair loop produces (pforces.cu:6-76);
+//   * integration, history shift, new-fluid detection and two-phase refill (move.cu:5-103,
+//     pforces.cu:80-116, refill.cu:8-240).
+// Geometric predicates use explicitly rounded double operations (__dmul_rn/__dadd_rn) so they
+// evaluate exactly like a non-contracted C implementation of the reference formulas.
+#include "rbtp_internal.cuh"
+
+namespace rbtp {
+
+namespace {
+
+constexpr double NEW_FLUID_THRESH = 1.7606816861659007;  // refill.cu:39,70
+
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+
+__device__ __forceinline__ double sq3(double dx, double dy, double dz)
+{
+    return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+}
+
+// links.cu:7-23 with explicit rounding
+__device__ __forceinline__ bool link_q(int cxi, int cyi, int czi, double x0, double y0, double z0,
+                                       double px, double py, double pz, double rsq, double &q)
+{
+    const double cxd = (double)cxi, cyd = (double)cyi, czd = (double)czi;
+    const double dx = dsub(x0, px), dy = dsub(y0, py), dz = dsub(z0, pz);
+    const double a = sq3(cxd, cyd, czd);
+    const double b = dmul(2.0, dadd(dadd(dmul(cxd, dx), dmul(cyd, dy)), dmul(czd, dz)));
+    const double c = dsub(sq3(dx, dy, dz), rsq);
+    const double disc = dsub(dmul(b, b), dmul(dmul(4.0, a), c));
+    if (disc <= 0.0) return false;
+    q = __ddiv_rn(dsub(-b, __dsqrt_rn(disc)), dmul(2.0, a));
+    return (q >= 0.0 && q <= 1.0);
+}
+
+// floor to int with the argument clamped first, so non-finite or far-away particle coordinates give
+// empty (clipped) boxes instead of overflowing integer arithmetic; NaN maps to -1e9.
+__device__ __forceinline__ int ifloor(double v)
+{
+    v = fmin(fmax(v, -1.0e9), 1.0e9);
+    return (int)floor(v);
+}
+
+#define PCOL(st, np, c, p) (st)[(long long)(c) * (np) + (p)]
+
+// Bounding box of links.cu:160-172: floor(p -/+ r - 0.5), clipped to the box.
+struct Box { int x0, x1, y0, y1, z0, z1; };
+
+__device__ __forceinline__ Box sphere_box(const Geo &geo, double px, double py, double pz,
+                                          double r, int pad)
+{
+    Box b;
+    b.x0 = ifloor(dsub(dsub(px, r), 0.5)) - pad;
+    b.x1 = ifloor(dsub(dadd(px, r), 0.5)) + pad;
+    b.y0 = ifloor(dsub(dsub(py, r), 0.5)) - pad;
+    b.y1 = ifloor(dsub(dadd(py, r), 0.5)) + pad;
+    b.z0 = ifloor(dsub(dsub(pz, r), 0.5)) - pad;
+    b.z1 = ifloor(dsub(dadd(pz, r), 0.5)) + pad;
+    if (b.x0 < 0) b.x0 = 0;
+    if (b.y0 < 0) b.y0 = 0;
+    if (b.z0 < 0) b.z0 = 0;
+    if (b.x1 > geo.lx - 1) b.x1 = geo.lx - 1;
+    if (b.y1 > geo.ly - 1) b.y1 = geo.ly - 1;
+    if (b.z1 > geo.lz - 1) b.z1 = geo.lz - 1;
+    return b;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Block reduction of NQ doubles in a fixed tree order (deterministic for a fixed block size).
+// ------------------------------------------------------------------------------------------------
+template <int NQ, int NT>
+__device__ __forceinline__ void block_reduce_fixed(double (&v)[NQ], double *sh /* NQ*NT */)
+{
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) sh[q * NT + t] = v[q];
+    __syncthreads();
+#pragma unroll
+    for (int s = NT / 2; s > 0; s >>= 1) {
+        if (t < s) {
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) sh[q * NT + t] += sh[q * NT + t + s];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) v[q] = sh[q * NT];
+}
+
+// ------------------------------------------------------------------------------------------------
+// IBB for f and g plus momentum exchange and heat flux, one CTA per particle.
+// ------------------------------------------------------------------------------------------------
+constexpr int IBB_THREADS = 128;
+
+template <int MODE>
+__global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const Phys ph,
+                                                           const PartBuffers pb, void *f_,
+                                                           void *g_, const double *rho)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    __shared__ double sh[7 * IBB_THREADS];
+    const int p = blockIdx.x;
+    const int np = pb.np;
+    S *fB = static_cast<S *>(f_);
+    S *gB = static_cast<S *>(g_);
+    const long long L = geo.L;
+    const double *st = pb.state;
+    const double px = PCOL(st, np, 0, p), py = PCOL(st, np, 1, p), pz = PCOL(st, np, 2, p);
+    const double vx = PCOL(st, np, 3, p), vy = PCOL(st, np, 4, p), vz = PCOL(st, np, 5, p);
+    const double wx = PCOL(st, np, 18, p), wy = PCOL(st, np, 19, p), wz = PCOL(st, np, 20, p);
+    const double Tp = PCOL(st, np, 30, p);
+    const int n = min(pb.link_cnt[p], pb.link_cap);
+    const long long base = (long long)p * pb.link_cap;
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    const double RT = 1.0 / 3.0;
+
+    for (int t = threadIdx.x; t < n; t += IBB_THREADS) {
+        const int x = pb.link_node[base + t];
+        const int ip = pb.link_dir[base + t];
+        const double q = pb.link_q[base + t];
+        const int iz = x / (int)geo.lxy;
+        const int rem = x - iz * (int)geo.lxy;
+        const int iy = rem / geo.lx;
+        const int ix = rem - iy * geo.lx;
+        const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
+        const int o = dopp_rt(ip);
+        const double w = dweight_rt(ip);
+        // moving wall velocity at the intersection point (ibb.cu:33-46)
+        const double cpx = (double)ix + 0.5 + q * cxi;
+        const double cpy = (double)iy + 0.5 + q * cyi;
+        const double cpz = (double)iz + 0.5 + q * czi;
+        const double relx = cpx - px, rely = cpy - py, relz = cpz - pz;
+        const double uwx = vx + (relz * wy - rely * wz);
+        const double uwy = vy + (relx * wz - relz * wx);
+        const double uwz = vz + (rely * wx - relx * wy);
+        const double evel = cxi * uwx + cyi * uwy + czi * uwz;
+        const double mom = 2.0 * w * ph.rho0 * evel / RT;
+
+        const int ix1 = ix - cxi, iy1 = iy - cyi, iz1 = iz - czi;
+        const bool in1 = ix1 >= 0 && ix1 < geo.lx && iy1 >= 0 && iy1 < geo.ly && iz1 >= 0 && iz1 < geo.lz;
+        const long long x1 = in1 ? ((long long)iz1 * geo.lxy + (long long)iy1 * geo.lx + ix1) : 0;
+        const bool fluid1 = in1 && pb.owner_cur[x1] < 0;
+
+        const double f_here = (double)ST::ld_f(fB + (long long)ip * L + x, w, ph.t0);
+        const double g_here = (double)ST::ld_g(gB + (long long)ip * L + x, w, ph.t0);
+        double fval, gval;
+        // ibb.cu:52-73 (f: q < 0.5), ibb.cu:114-128 (g: q <= 0.5)
+        if (fluid1) {
+            if (q < 0.5) {
+                const double f_up = (double)ST::ld_f(fB + (long long)ip * L + x1, w, ph.t0);
+                fval = 2.0 * q * f_here + (1.0 - 2.0 * q) * f_up - mom;
+            } else {
+                const double f_oc = (double)ST::ld_f(fB + (long long)o * L + x, w, ph.t0);
+                const double inv_2q = 0.5 / q;
+                fval = (f_here - mom) * inv_2q + (2.0 * q - 1.0) * inv_2q * f_oc;
+            }
+        } else {
+            fval = f_here - mom;
+        }
+        const double amp = 2.0 * w * Tp * (1.0 + rho[x]);
+        if (fluid1) {
+            if (q <= 0.5) {
+                const double gu = (double)ST::ld_g(gB + (long long)ip * L + x1, w, ph.t0);
+                gval = -(2.0 * q * g_here + (1.0 - 2.0 * q) * gu) + amp;
+            } else {
+                const double go = (double)ST::ld_g(gB + (long long)o * L + x, w, ph.t0);
+                const double inv_2q = 0.5 / q;
+                gval = -g_here * inv_2q + amp * inv_2q + (2.0 * q - 1.0) * inv_2q * go;
+            }
+        } else {
+            gval = -g_here + amp;
+        }
+        // The population that streams into x along opp comes from the solid node x + c_ip: the
+        // pull of the next step reads it from slot (opp, x + c_ip).
+        const long long solid = (long long)x + cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
+        ST::st_f(fB + (long long)o * L + solid, (typename ST::R)fval, w, ph.t0);
+        ST::st_g(gB + (long long)o * L + solid, (typename ST::R)gval, w, ph.t0);
+        // In FP32/FP16 storage the value the reference would read back is the rounded one.
+        const double f_out = (MODE == RBTP_STORE_F64) ? fval
+                              : (double)ST::ld_f(fB + (long long)o * L + solid, w, ph.t0);
+        const double g_out = (MODE == RBTP_STORE_F64) ? gval
+                              : (double)ST::ld_g(gB + (long long)o * L + solid, w, ph.t0);
+        // ibb.cu:160-187 (force, torque) and 202-204 (heat)
+        const double crx = (double)ix + 0.5 + q * (double)cxi;
+        const double cry = (double)iy + 0.5 + q * (double)cyi;
+        const double crz = (double)iz + 0.5 + q * (double)czi;
+        const double rx = crx - px, ry = cry - py, rz = crz - pz;
+        const double Fx = (cxi - uwx) * f_here - (-cxi - uwx) * f_out;
+        const double Fy = (cyi - uwy) * f_here - (-cyi - uwy) * f_out;
+        const double Fz = (czi - uwz) * f_here - (-czi - uwz) * f_out;
+        acc[0] += Fx;
+        acc[1] += Fy;
+        acc[2] += Fz;
+        acc[3] += ry * Fz - rz * Fy;
+        acc[4] += rz * Fx - rx * Fz;
+        acc[5] += rx * Fy - ry * Fx;
+        acc[6] += g_here - g_out;
+    }
+    block_reduce_fixed<7, IBB_THREADS>(acc, sh);
+    if (threadIdx.x == 0) {
+        pb.hF[p] = acc[0]; pb.hF[np + p] = acc[1]; pb.hF[2 * np + p] = acc[2];
+        pb.hT[p] = acc[3]; pb.hT[np + p] = acc[4]; pb.hT[2 * np + p] = acc[5];
+        pb.hQ[p] = acc[6];
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Contacts: cell list, ascending-partner sums (pforces.cu:6-76).
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ int cell_of(double v, double cs, int n)
+{
+    int c = ifloor(v / cs);
+    if (c < 0) c = 0;
+    if (c > n - 1) c = n - 1;
+    return c;
+}
+
+__global__ void k_cell_count(const PartBuffers pb)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= pb.np) return;
+    const double *st = pb.state;
+    const int cx = cell_of(PCOL(st, pb.np, 0, p), pb.cell_size, pb.ncell[0]);
+    const int cy = cell_of(PCOL(st, pb.np, 1, p), pb.cell_size, pb.ncell[1]);
+    const int cz = cell_of(PCOL(st, pb.np, 2, p), pb.cell_size, pb.ncell[2]);
+    atomicAdd(&pb.cell_count[(cz * pb.ncell[1] + cy) * pb.ncell[0] + cx], 1);
+}
+
+__global__ void k_cell_scan(const PartBuffers pb, int ncells)
+{
+    // single block; sequential chunks with a block scan
+    __shared__ int sh[1024];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int b = 0; b < ncells; b += blockDim.x) {
+        const int i = b + threadIdx.x;
+        const int v = i < ncells ? pb.cell_count[i] : 0;
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int off = 1; off < (int)blockDim.x; off <<= 1) {
+            const int add = threadIdx.x >= (unsigned)off ? sh[threadIdx.x - off] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += add;
+            __syncthreads();
+        }
+        if (i < ncells) pb.cell_start[i] = carry + sh[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += sh[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+__global__ void k_cell_fill(const PartBuffers pb)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= pb.np) return;
+    const double *st = pb.state;
+    const int cx = cell_of(PCOL(st, pb.np, 0, p), pb.cell_size, pb.ncell[0]);
+    const int cy = cell_of(PCOL(st, pb.np, 1, p), pb.cell_size, pb.ncell[1]);
+    const int cz = cell_of(PCOL(st, pb.np, 2, p), pb.cell_size, pb.ncell[2]);
+    const int c = (cz * pb.ncell[1] + cy) * pb.ncell[0] + cx;
+    const int slot = atomicAdd(&pb.cell_fill[c], 1);
+    pb.cell_items[pb.cell_start[c] + slot] = p;
+}
+
+constexpr int MAX_CAND = 64;
+
+__global__ void k_contact_force(const Geo geo, const Phys ph, const PartBuffers pb,
+                                DevStatus *status)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int np = pb.np;
+    if (p >= np) return;
+    const double *st = pb.state;
+    const double x = PCOL(st, np, 0, p), y = PCOL(st, np, 1, p), z = PCOL(st, np, 2, p);
+    const double radius = ph.radius, coeff = ph.rep_coeff, min_gap = ph.min_gap;
+    int cand[MAX_CAND];
+    int nc = 0;
+    if (np > 1) {
+        const int cx = cell_of(x, pb.cell_size, pb.ncell[0]);
+        const int cy = cell_of(y, pb.cell_size, pb.ncell[1]);
+        const int cz = cell_of(z, pb.cell_size, pb.ncell[2]);
+        for (int kz = max(cz - 1, 0); kz <= min(cz + 1, pb.ncell[2] - 1); ++kz)
+            for (int ky = max(cy - 1, 0); ky <= min(cy + 1, pb.ncell[1] - 1); ++ky)
+                for (int kx = max(cx - 1, 0); kx <= min(cx + 1, pb.ncell[0] - 1); ++kx) {
+                    const int c = (kz * pb.ncell[1] + ky) * pb.ncell[0] + kx;
+                    const int s0 = pb.cell_start[c], s1 = s0 + pb.cell_count[c];
+                    for (int s = s0; s < s1; ++s) {
+                        const int q = pb.cell_items[s];
+                        if (q == p) continue;
+                        const double dx = dsub(x, PCOL(st, np, 0, q));
+                        const double dy = dsub(y, PCOL(st, np, 1, q));
+                        const double dz = dsub(z, PCOL(st, np, 2, q));
+                        const double dsq = sq3(dx, dy, dz);
+                        if (dsq <= 1.0e-12) continue;
+                        const double hgap = dsub(__dsqrt_rn(dsq), dmul(2.0, radius));
+                        if (hgap >= min_gap) continue;
+                        if (nc < MAX_CAND) cand[nc++] = q;
+                        else atomicOr(&status->contact_overflow, 1);
+                    }
+                }
+        // ascending partner order = the order pforces.cu's pair loop adds them to p
+        for (int i = 1; i < nc; ++i) {
+            const int v = cand[i];
+            int j = i - 1;
+            while (j >= 0 && cand[j] > v) { cand[j + 1] = cand[j]; --j; }
+            cand[j + 1] = v;
+        }
+    }
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    for (int i = 0; i < nc; ++i) {
+        const int q = cand[i];
+        const double dx = dsub(x, PCOL(st, np, 0, q));
+        const double dy = dsub(y, PCOL(st, np, 1, q));
+        const double dz = dsub(z, PCOL(st, np, 2, q));
+        const double dist = __dsqrt_rn(sq3(dx, dy, dz));
+        const double hgap = dsub(dist, dmul(2.0, radius));
+        const double overlap = (hgap < 0.0) ? -hgap : 0.0;
+        const double factor = __ddiv_rn(dsub(min_gap, hgap), min_gap);
+        const double lub = dmul(coeff, dadd(__ddiv_rn(dmul(factor, factor), ph.stf0),
+                                            __ddiv_rn(overlap, dmul(min_gap, ph.stf1))));
+        fx = dadd(fx, dmul(lub, __ddiv_rn(dx, dist)));
+        fy = dadd(fy, dmul(lub, __ddiv_rn(dy, dist)));
+        fz = dadd(fz, dmul(lub, __ddiv_rn(dz, dist)));
+        if (q > p) {
+            const int slot = atomicAdd(&status->ncontacts, 1);
+            if (slot < pb.pair_cap) { pb.pair_p[slot] = p; pb.pair_q[slot] = q; }
+        }
+    }
+    // walls (pforces.cu:40-76)
+    double wfx = 0.0, wfy = 0.0, wfz = 0.0;
+    const double gaps[6] = {dsub(x, radius), dsub(dsub((double)geo.lx, x), radius),
+                            dsub(y, radius), dsub(dsub((double)geo.ly, y), radius),
+                            dsub(z, radius), dsub(dsub((double)geo.lz, z), radius)};
+    const double mgw = ph.min_gap_w;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const double gap = gaps[k];
+        if (gap >= mgw) continue;
+        const double overlap = (gap < 0.0) ? -gap : 0.0;
+        const double factor = __ddiv_rn(dsub(mgw, gap), mgw);
+        const double lub = dmul(coeff, dadd(__ddiv_rn(dmul(factor, factor), ph.stf0_w),
+                                            __ddiv_rn(overlap, dmul(mgw, ph.stf1_w))));
+        // wall normals +x, -x, +y, -y, +z, -z; the zero components add +0.0 and are skipped
+        const double sgn = (k & 1) ? -1.0 : 1.0;
+        if (k < 2) wfx = dadd(wfx, dmul(lub, sgn));
+        else if (k < 4) wfy = dadd(wfy, dmul(lub, sgn));
+        else wfz = dadd(wfz, dmul(lub, sgn));
+    }
+    pb.cF[p] = dadd(fx, wfx);
+    pb.cF[np + p] = dadd(fy, wfy);
+    pb.cF[2 * np + p] = dadd(fz, wfz);
+}
+
+// ------------------------------------------------------------------------------------------------
+// History shift + Newton-Euler + temperature (pforces.cu:80-116, ibb.cu:258-262, move.cu:5-103).
+// ------------------------------------------------------------------------------------------------
+__global__ void k_update(const Phys ph, const PartBuffers pb)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int np = pb.np;
+    if (p >= np) return;
+    double *st = pb.state;
+    const double dt = 1.0;
+    const double buoyancy = (1.0 - 1.0 / ph.rho_ratio) * ph.grav0;
+    double vn[3], on[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        // force / torque histories: prev2 <- prev, prev <- accum, accum <- this step's sums
+        const double f_prev = PCOL(st, np, 6 + a, p);
+        const double f_prev2 = PCOL(st, np, 9 + a, p);
+        const double t_prev = PCOL(st, np, 21 + a, p);
+        const double t_prev2 = PCOL(st, np, 24 + a, p);
+        const double f_now = pb.cF[a * np + p] + pb.hF[a * np + p];
+        const double t_now = pb.hT[a * np + p];
+        PCOL(st, np, 12 + a, p) = f_prev2;
+        PCOL(st, np, 9 + a, p) = f_prev;
+        PCOL(st, np, 6 + a, p) = f_now;
+        PCOL(st, np, 27 + a, p) = t_prev2;
+        PCOL(st, np, 24 + a, p) = t_prev;
+        PCOL(st, np, 21 + a, p) = t_now;
+        const double combo_f = 0.5 * f_now + f_prev + 0.5 * f_prev2;
+        const double combo_t = 0.5 * t_now + t_prev + 0.5 * t_prev2;
+        vn[a] = PCOL(st, np, 3 + a, p) + 0.5 * dt * combo_f / ph.mass;
+        if (a == 0) vn[a] += dt * buoyancy;
+        on[a] = PCOL(st, np, 18 + a, p) + 0.5 * dt * combo_t / ph.inertia;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        PCOL(st, np, a, p) = PCOL(st, np, a, p) + 0.5 * dt * (vn[a] + PCOL(st, np, 3 + a, p));
+        PCOL(st, np, 15 + a, p) = PCOL(st, np, 15 + a, p) + 0.5 * dt * (on[a] + PCOL(st, np, 18 + a, p));
+        PCOL(st, np, 3 + a, p) = vn[a];
+        PCOL(st, np, 18 + a, p) = on[a];
+    }
+    const double heat_prev = PCOL(st, np, 31, p);
+    const double heat = pb.hQ[p];
+    PCOL(st, np, 32, p) = heat_prev;
+    PCOL(st, np, 31, p) = heat;
+    PCOL(st, np, 30, p) = PCOL(st, np, 30, p) + 0.5 * dt * (heat + heat_prev) / ph.heat_cap;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Solid marking over all particles (links.cu:25-48, 160-188).
+// ------------------------------------------------------------------------------------------------
+__global__ void k_mark(const Geo geo, const Phys ph, const PartBuffers pb, int *owner)
+{
+    const int p = blockIdx.x;
+    const double *st = pb.state;
+    const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
+    const double r = ph.radius;
+    const double rsq = dmul(r, r);
+    const Box b = sphere_box(geo, px, py, pz, r, 0);
+    if (b.x0 > b.x1 || b.y0 > b.y1 || b.z0 > b.z1) return;
+    const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
+    const int total = nx * ny * nz;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int lz = t / (nx * ny);
+        const int rem = t - lz * nx * ny;
+        const int ly = rem / nx;
+        const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
+        const double dx = dsub((double)ix + 0.5, px);
+        const double dy = dsub((double)iy + 0.5, py);
+        const double dz = dsub((double)iz + 0.5, pz);
+        if (sq3(dx, dy, dz) > rsq) continue;
+        const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
+        atomicMin(reinterpret_cast<unsigned int *>(owner) + idx, (unsigned int)p);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Link slabs (links.cu:50-139): CTA per particle, ordered compaction over its padded box.
+// ------------------------------------------------------------------------------------------------
+constexpr int LINK_THREADS = 256;
+
+__global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const Phys ph,
+                                                            const PartBuffers pb, const int *owner,
+                                                            DevStatus *status)
+{
+    __shared__ int wsum[LINK_THREADS / 32];
+    __shared__ int base_sh;
+    const int p = blockIdx.x;
+    const double *st = pb.state;
+    const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
+    const double r = ph.radius;
+    const double rsq = dmul(r, r);
+    const Box b = sphere_box(geo, px, py, pz, r, 1);
+    const long long slab = (long long)p * pb.link_cap;
+    if (threadIdx.x == 0) base_sh = 0;
+    __syncthreads();
+    if (b.x0 > b.x1 || b.y0 > b.y1 || b.z0 > b.z1) {
+        if (threadIdx.x == 0) pb.link_cnt[p] = 0;
+        return;
+    }
+    const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
+    const int total = nx * ny * nz;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c0 = 0; c0 < total; c0 += LINK_THREADS) {
+        const int t = c0 + threadIdx.x;
+        unsigned mask = 0;
+        int ix = 0, iy = 0, iz = 0;
+        double qv[26];
+        if (t < total) {
+            const int lz = t / (nx * ny);
+            const int rem = t - lz * nx * ny;
+            const int ly = rem / nx;
+            ix = b.x0 + (rem - ly * nx); iy = b.y0 + ly; iz = b.z0 + lz;
+            const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
+            if (owner[idx] < 0) {
+                const double x0 = (double)ix + 0.5, y0 = (double)iy + 0.5, z0 = (double)iz + 0.5;
+                unroll<26>([&](auto K) {
+                    constexpr int ip = decltype(K)::value + 1;
+                    constexpr int cx = dcx(ip), cy = dcy(ip), cz = dcz(ip);
+                    const int xn = ix + cx, yn = iy + cy, zn = iz + cz;
+                    if (xn >= 0 && xn < geo.lx && yn >= 0 && yn < geo.ly && zn >= 0 && zn < geo.lz) {
+                        const long long nidx = (long long)zn * geo.lxy + (long long)yn * geo.lx + xn;
+                        if (owner[nidx] == p) {
+                            double q;
+                            if (link_q(cx, cy, cz, x0, y0, z0, px, py, pz, rsq, q)) {
+                                mask |= 1u << (ip - 1);
+                                qv[ip - 1] = q;
+                            }
+                        }
+                    }
+                });
+            }
+        }
+        const int cnt = __popc(mask);
+        // block exclusive scan of cnt in thread order (= node index order)
+        int incl = cnt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += v;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        int wbase = 0, ctotal = 0;
+        for (int k = 0; k < LINK_THREADS / 32; ++k) {
+            if (k < warp) wbase += wsum[k];
+            ctotal += wsum[k];
+        }
+        int pos = base_sh + wbase + incl - cnt;
+        if (mask) {
+            const long long node = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
+            unroll<26>([&](auto K) {
+                constexpr int ip = decltype(K)::value + 1;
+                if (mask & (1u << (ip - 1))) {
+                    if (pos < pb.link_cap) {
+                        pb.link_node[slab + pos] = (int)node;
+                        pb.link_dir[slab + pos] = ip;
+                        pb.link_q[slab + pos] = qv[ip - 1];
+                    } else {
+                        atomicOr(&status->link_overflow, 1);
+                    }
+                    ++pos;
+                }
+            });
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) base_sh += ctotal;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) pb.link_cnt[p] = base_sh;
+}
+
+// ------------------------------------------------------------------------------------------------
+// New-fluid detection (refill.cu:8-76), per particle around its new position.
+// ------------------------------------------------------------------------------------------------
+__global__ void k_new_fluid(const Geo geo, const Phys ph, const PartBuffers pb,
+                            const int *owner_prev, const int *owner_cur, DevStatus *status)
+{
+    const int p = blockIdx.x;
+    const double *st = pb.state;
+    const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
+    const double r = ph.radius;
+    const Box b = sphere_box(geo, px, py, pz, dadd(r, NEW_FLUID_THRESH), 1);
+    if (b.x0 > b.x1 || b.y0 > b.y1 || b.z0 > b.z1) return;
+    const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
+    const int total = nx * ny * nz;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int lz = t / (nx * ny);
+        const int rem = t - lz * nx * ny;
+        const int ly = rem / nx;
+        const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
+        const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
+        if (owner_prev[idx] != p || owner_cur[idx] >= 0) continue;
+        const double dx = dsub((double)ix + 0.5, px);
+        const double dy = dsub((double)iy + 0.5, py);
+        const double dz = dsub((double)iz + 0.5, pz);
+        const double dist = __dsqrt_rn(sq3(dx, dy, dz));
+        if (dsub(dist, r) > NEW_FLUID_THRESH) continue;
+        const int slot = atomicAdd(&status->nf_count, 1);
+        if (slot < pb.nf_cap) { pb.nf_node[slot] = (int)idx; pb.nf_pid[slot] = p; }
+        else atomicOr(&status->nf_overflow, 1);
+    }
+}
+
+// Refill values (refill.cu:78-240): one warp per new-fluid node, lane ip computes population ip
+// from the post-collision populations of previous-step fluid neighbours (home slots of the
+// buffer just written by the step kernel).
+template <int MODE>
+__global__ void k_refill_compute(const Geo geo, const Phys ph, const PartBuffers pb,
+                                 const int *owner_prev, const void *f_, const void *g_,
+                                 const DevStatus *status)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    const S *fB = static_cast<const S *>(f_);
+    const S *gB = static_cast<const S *>(g_);
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int count = min(status->nf_count, pb.nf_cap);
+    const long long L = geo.L;
+    const double RT = 1.0 / 3.0;
+    const double lambda0 = 1.0 - dweight(0);
+    for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < count; n += nwarps) {
+        const int idx = pb.nf_node[n];
+        const int iz = idx / (int)geo.lxy;
+        const int iy = (idx - iz * (int)geo.lxy) / geo.lx;
+        const int ix = idx - iz * (int)geo.lxy - iy * geo.lx;
+        int pid = pb.nf_pid[n];
+        if (pid < 0) {
+            const int pp = owner_prev[idx];
+            if (pp >= 0) pid = pp;
+        }
+        double fv = 0.0, gv = 0.0;
+        if (lane < 27) {
+            const int ip = lane;
+            const double w = dweight_rt(ip);
+            double tf = 0.0, tg = 0.0;
+            int sc = 0;
+            for (int ip2 = 1; ip2 < 27; ++ip2) {
+                const int cx2 = dcx_rt(ip2), cy2 = dcy_rt(ip2), cz2 = dcz_rt(ip2);
+                const int x1 = ix + cx2, y1 = iy + cy2, z1 = iz + cz2;
+                if (x1 < 0 || x1 >= geo.lx || y1 < 0 || y1 >= geo.ly || z1 < 0 || z1 >= geo.lz) continue;
+                const long long i1 = (long long)z1 * geo.lxy + (long long)y1 * geo.lx + x1;
+                if (owner_prev[i1] >= 0) continue;
+                const int x2 = ix + 2 * cx2, y2 = iy + 2 * cy2, z2 = iz + 2 * cz2;
+                const bool in2 = x2 >= 0 && x2 < geo.lx && y2 >= 0 && y2 < geo.ly && z2 >= 0 && z2 < geo.lz;
+                const double f1 = (double)ST::ld_f(fB + (long long)ip * L + i1, w, ph.t0);
+                const double g1 = (double)ST::ld_g(gB + (long long)ip * L + i1, w, ph.t0);
+                if (in2) {
+                    const long long i2 = (long long)z2 * geo.lxy + (long long)y2 * geo.lx + x2;
+                    if (owner_prev[i2] < 0) {
+                        tf += 2.0 * f1 - (double)ST::ld_f(fB + (long long)ip * L + i2, w, ph.t0);
+                        tg += 2.0 * g1 - (double)ST::ld_g(gB + (long long)ip * L + i2, w, ph.t0);
+                        ++sc;
+                        continue;
+                    }
+                }
+                tf += f1;
+                tg += g1;
+                ++sc;
+            }
+            if (sc == 0) {
+                double px = 0, py = 0, pz = 0, vx = 0, vy = 0, vz = 0, wx = 0, wy = 0, wz = 0;
+                double tT = ph.t0;
+                const double *st = pb.state;
+                if (pid >= 0) {
+                    px = PCOL(st, pb.np, 0, pid); py = PCOL(st, pb.np, 1, pid); pz = PCOL(st, pb.np, 2, pid);
+                    vx = PCOL(st, pb.np, 3, pid); vy = PCOL(st, pb.np, 4, pid); vz = PCOL(st, pb.np, 5, pid);
+                    wx = PCOL(st, pb.np, 18, pid); wy = PCOL(st, pb.np, 19, pid); wz = PCOL(st, pb.np, 20, pid);
+                    tT = PCOL(st, pb.np, 30, pid);
+                }
+                const double relx = ((double)ix + 0.5) - px;
+                const double rely = ((double)iy + 0.5) - py;
+                const double relz = ((double)iz + 0.5) - pz;
+                double u = vx + (relz * wy - rely * wz);
+                double v = vy + (relx * wz - relz * wx);
+                double ww = vz + (rely * wx - relx * wy);
+                if (pid < 0) { u = 0.0; v = 0.0; ww = 0.0; }
+                const double r = ph.rho0;
+                // refill.cu:196-201: eu is c.u without the 1/RT factor
+                const double eu = dcx_rt(ip) * u + dcy_rt(ip) * v + dcz_rt(ip) * ww;
+                const double uv = (u * u + v * v + ww * ww) / RT;
+                tf = w * (r + eu + 0.5 * (eu * eu - uv));
+                tg = w * tT * (1.0 + eu + 0.5 * (eu * eu - uv));
+                if (ip == 0) tg -= lambda0 * tT * r;
+                else tg += w * tT * r;
+                sc = 1;
+            }
+            const double inv = 1.0 / (double)sc;
+            fv = tf * inv;
+            gv = tg * inv;
+            pb.nf_val[(long long)n * 54 + ip] = fv;
+            pb.nf_val[(long long)n * 54 + 27 + ip] = gv;
+        }
+        // node macros in population order (refill.cu:226-239), lane 0
+        double rho_loc = 0, mx = 0, my = 0, mz = 0, phi_loc = 0;
+        for (int ip = 0; ip < 27; ++ip) {
+            const double a = __shfl_sync(0xffffffffu, fv, ip);
+            const double c = __shfl_sync(0xffffffffu, gv, ip);
+            rho_loc += a;
+            mx += dcx_rt(ip) * a;
+            my += dcy_rt(ip) * a;
+            mz += dcz_rt(ip) * a;
+            phi_loc += c;
+        }
+        if (lane == 0) {
+            double *m = pb.nf_mac + (long long)n * 5;
+            m[0] = rho_loc;
+            if (rho_loc > 1e-12) {
+                const double inv_rho = 1.0 / rho_loc;
+                m[1] = mx * inv_rho; m[2] = my * inv_rho; m[3] = mz * inv_rho;
+            } else {
+                m[1] = 0.0; m[2] = 0.0; m[3] = 0.0;
+            }
+            m[4] = phi_loc;
+        }
+    }
+}
+
+// Scatter the refill values into the slots the next pull reads at each new-fluid node.
+template <int MODE>
+__global__ void k_refill_scatter(const Geo geo, const Phys ph, const PartBuffers pb, void *f_,
+                                 void *g_, double *faux, const double *rho_wall, bool macros,
+                                 double *rho, double *ux, double *uy, double *uz, double *phi,
+                                 const DevStatus *status)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    using R = typename ST::R;
+    S *fB = static_cast<S *>(f_);
+    S *gB = static_cast<S *>(g_);
+    const int count = min(status->nf_count, pb.nf_cap);
+    const long long L = geo.L;
+    const long long total = (long long)count * 27;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int n = (int)(t / 27);
+        const int ip = (int)(t - (long long)n * 27);
+        const int idx = pb.nf_node[n];
+        const int iz = idx / (int)geo.lxy;
+        const int iy = (idx - iz * (int)geo.lxy) / geo.lx;
+        const int ix = idx - iz * (int)geo.lxy - iy * geo.lx;
+        const int cx = dcx_rt(ip), cy = dcy_rt(ip), cz = dcz_rt(ip), o = dopp_rt(ip);
+        const double w = dweight_rt(ip);
+        const double fv = pb.nf_val[(long long)n * 54 + ip];
+        const double gv = pb.nf_val[(long long)n * 54 + 27 + ip];
+        const bool ox = (cx == 1 && ix == 0) || (cx == -1 && ix == geo.lx - 1);
+        const bool oy = (cy == 1 && iy == 0) || (cy == -1 && iy == geo.ly - 1);
+        const bool oz = (cz == 1 && iz == 0) || (cz == -1 && iz == geo.lz - 1);
+        if (!(ox || oy || oz)) {
+            const long long src = (long long)idx - cx - (long long)cy * geo.lx - (long long)cz * geo.lxy;
+            ST::st_f(fB + (long long)ip * L + src, (R)fv, w, ph.t0);
+            ST::st_g(gB + (long long)ip * L + src, (R)gv, w, ph.t0);
+        } else {
+            ST::st_f(fB + (long long)o * L + idx, (R)fv, w, ph.t0);
+            double gs = gv;
+            if (ox && !oy && !oz) {
+                // the pull applies g <- -stored + 2 w T_wall (1 + rho_wall); store its preimage
+                const double tw = (cx == 1) ? ph.thot : ph.tcold;
+                const long long ws = (long long)iz * geo.ly + iy + (cx == 1 ? 0 : (long long)geo.lz * geo.ly);
+                gs = 2.0 * w * tw * (1.0 + rho_wall[ws]) - gv;
+            }
+            ST::st_g(gB + (long long)o * L + idx, (R)gs, w, ph.t0);
+        }
+        if (ip == 0) {
+            faux[idx] = 0.0;
+            if (macros) {
+                const double *m = pb.nf_mac + (long long)n * 5;
+                rho[idx] = m[0]; ux[idx] = m[1]; uy[idx] = m[2]; uz[idx] = m[3]; phi[idx] = m[4];
+            }
+        }
+    }
+}
+
+}  // namespace
+
+#define RBTP_MODE_DISPATCH(mode, CALL)                                      \
+    switch (mode) {                                                         \
+    case RBTP_STORE_F64: { constexpr int M = RBTP_STORE_F64; CALL; break; }  \
+    case RBTP_STORE_F32: { constexpr int M = RBTP_STORE_F32; CALL; break; }  \
+    case RBTP_STORE_F16S: { constexpr int M = RBTP_STORE_F16S; CALL; break; } \
+    default: return cudaErrorInvalidValue;                                  \
+    }
+
+cudaError_t launch_links_ibb(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                             void *f, void *g, const double *rho, cudaStream_t st)
+{
+    if (pb.np <= 0) return cudaSuccess;
+    RBTP_MODE_DISPATCH(mode, (k_links_ibb<M><<<pb.np, IBB_THREADS, 0, st>>>(geo, ph, pb, f, g, rho)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_contacts(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                            DevStatus *status, cudaStream_t st)
+{
+    if (pb.np <= 0) return cudaSuccess;
+    const int ncells = pb.ncell[0] * pb.ncell[1] * pb.ncell[2];
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(pb.cell_count, 0, sizeof(int) * ncells, st))) return e;
+    if ((e = cudaMemsetAsync(pb.cell_fill, 0, sizeof(int) * ncells, st))) return e;
+    if ((e = cudaMemsetAsync(&status->ncontacts, 0, sizeof(int), st))) return e;
+    const int t = 128, bl = (pb.np + t - 1) / t;
+    k_cell_count<<<bl, t, 0, st>>>(pb);
+    k_cell_scan<<<1, 1024, 0, st>>>(pb, ncells);
+    k_cell_fill<<<bl, t, 0, st>>>(pb);
+    k_contact_force<<<bl, t, 0, st>>>(geo, ph, pb, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_update(const Phys &ph, const PartBuffers &pb, cudaStream_t st)
+{
+    if (pb.np <= 0) return cudaSuccess;
+    k_update<<<(pb.np + 127) / 128, 128, 0, st>>>(ph, pb);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_mark(const Geo &geo, const Phys &ph, const PartBuffers &pb, int *owner_out,
+                        cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(owner_out, 0xFF, sizeof(int) * (size_t)geo.L, st);
+    if (e) return e;
+    if (pb.np <= 0) return cudaSuccess;
+    k_mark<<<pb.np, 256, 0, st>>>(geo, ph, pb, owner_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_initial_owner(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                                 int *owner, cudaStream_t st)
+{
+    return launch_mark(geo, ph, pb, owner, st);
+}
+
+cudaError_t launch_link_fill(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                             const int *owner, DevStatus *status, cudaStream_t st)
+{
+    if (pb.np <= 0) return cudaSuccess;
+    k_link_fill<<<pb.np, LINK_THREADS, 0, st>>>(geo, ph, pb, owner, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                          const int *owner_prev, const int *owner_cur, void *f, void *g,
+                          double *faux, const double *rho_wall, bool macros, double *rho,
+                          double *ux, double *uy, double *uz, double *phi, DevStatus *status,
+                          cudaStream_t st)
+{
+    if (pb.np <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(&status->nf_count, 0, sizeof(int), st);
+    if (e) return e;
+    k_new_fluid<<<pb.np, 256, 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
+    RBTP_MODE_DISPATCH(mode, (k_refill_compute<M><<<152, 256, 0, st>>>(geo, ph, pb, owner_prev, f, g, status)));
+    RBTP_MODE_DISPATCH(mode, (k_refill_scatter<M><<<152, 256, 0, st>>>(geo, ph, pb, f, g, faux, rho_wall, macros, rho, ux, uy, uz, phi, status)));
+    return cudaGetLastError();
+}
+
+}  // namespace rbtp

@@ -1,0 +1,240 @@
+// rbtp_internal.cuh — shared device/host definitions of librbtp (GB300, sm_103a).
+//
+// Lattice: D3Q27 in the reference's direction order (src_lbm/initial.cu:276-286) so that every
+// exported array has the reference layout.  The tables are compile-time constants: kernels unroll
+// over directions with std::integer_sequence so each direction's velocity, weight and opposite fold
+// into the instruction stream instead of being read from constant memory.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/rbtp.h"
+
+namespace rbtp {
+
+// ------------------------------------------------------------------------------------------------
+// D3Q27 tables (initial.cu:276-286)
+// ------------------------------------------------------------------------------------------------
+__host__ __device__ constexpr int dcx(int i)
+{
+    constexpr int t[27] = {0, 1, 0, -1, 0, 0, 0, 1, -1, -1, 1, 1, 0, -1, 0, 1, 0, -1, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+    return t[i];
+}
+__host__ __device__ constexpr int dcy(int i)
+{
+    constexpr int t[27] = {0, 0, 1, 0, -1, 0, 0, 1, 1, -1, -1, 0, 1, 0, -1, 0, 1, 0, -1, 1, 1, -1, -1, 1, 1, -1, -1};
+    return t[i];
+}
+__host__ __device__ constexpr int dcz(int i)
+{
+    constexpr int t[27] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, 1, 1, -1, -1, -1, -1, 1, 1, 1, 1, -1, -1, -1, -1};
+    return t[i];
+}
+__host__ __device__ constexpr int dopp(int i)
+{
+    constexpr int t[27] = {0, 3, 4, 1, 2, 6, 5, 9, 10, 7, 8, 17, 18, 15, 16, 13, 14, 11, 12, 25, 26, 23, 24, 21, 22, 19, 20};
+    return t[i];
+}
+// weight class: 0 rest, 1 face (2/27), 2 edge (1/54), 3 corner (1/216)
+__host__ __device__ constexpr int dclass(int i) { return i == 0 ? 0 : (i <= 6 ? 1 : (i <= 18 ? 2 : 3)); }
+__host__ __device__ constexpr double dweight(int i)
+{
+    return i == 0 ? 8.0 / 27.0 : (i <= 6 ? 2.0 / 27.0 : (i <= 18 ? 1.0 / 54.0 : 1.0 / 216.0));
+}
+// the 13 direction pairs (i, opp(i)) with i < opp(i)
+__host__ __device__ constexpr int dpair(int k)
+{
+    constexpr int t[13] = {1, 2, 5, 7, 8, 11, 12, 13, 14, 19, 20, 21, 22};
+    return t[k];
+}
+
+// Runtime-indexed copies of the tables for loops that are not unrolled (sparse particle work).
+static __constant__ int c_cx[27] = {0, 1, 0, -1, 0, 0, 0, 1, -1, -1, 1, 1, 0, -1, 0, 1, 0, -1, 0, 1, -1, -1, 1, 1, -1, -1, 1};
+static __constant__ int c_cy[27] = {0, 0, 1, 0, -1, 0, 0, 1, 1, -1, -1, 0, 1, 0, -1, 0, 1, 0, -1, 1, 1, -1, -1, 1, 1, -1, -1};
+static __constant__ int c_cz[27] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, 1, 1, -1, -1, -1, -1, 1, 1, 1, 1, -1, -1, -1, -1};
+static __constant__ int c_opp[27] = {0, 3, 4, 1, 2, 6, 5, 9, 10, 7, 8, 17, 18, 15, 16, 13, 14, 11, 12, 25, 26, 23, 24, 21, 22, 19, 20};
+__device__ __forceinline__ int dcx_rt(int i) { return c_cx[i]; }
+__device__ __forceinline__ int dcy_rt(int i) { return c_cy[i]; }
+__device__ __forceinline__ int dcz_rt(int i) { return c_cz[i]; }
+__device__ __forceinline__ int dopp_rt(int i) { return c_opp[i]; }
+__device__ __forceinline__ double dweight_rt(int i)
+{
+    return i == 0 ? 8.0 / 27.0 : (i <= 6 ? 2.0 / 27.0 : (i <= 18 ? 1.0 / 54.0 : 1.0 / 216.0));
+}
+
+template <class F, int... Is>
+__host__ __device__ __forceinline__ void unroll_impl(F &&f, std::integer_sequence<int, Is...>)
+{
+    (f(std::integral_constant<int, Is>()), ...);
+}
+template <int N, class F>
+__host__ __device__ __forceinline__ void unroll(F &&f)
+{
+    unroll_impl(f, std::make_integer_sequence<int, N>());
+}
+
+// ------------------------------------------------------------------------------------------------
+// Population storage modes.  R is the arithmetic type of the collision, S the storage type.
+// FP16 mode stores (pop / w_i) for f (the deviation-form f needs no shift) and (g / w_i - T0) for g.
+// ------------------------------------------------------------------------------------------------
+template <int MODE> struct Store;
+template <> struct Store<RBTP_STORE_F64> {
+    using S = double;
+    using R = double;
+    static __device__ __forceinline__ R ld_f(const S *p, double, double) { return *p; }
+    static __device__ __forceinline__ R ld_g(const S *p, double, double) { return *p; }
+    static __device__ __forceinline__ void st_f(S *p, R v, double, double) { *p = v; }
+    static __device__ __forceinline__ void st_g(S *p, R v, double, double) { *p = v; }
+};
+template <> struct Store<RBTP_STORE_F32> {
+    using S = float;
+    using R = float;
+    static __device__ __forceinline__ R ld_f(const S *p, double, double) { return *p; }
+    static __device__ __forceinline__ R ld_g(const S *p, double, double) { return *p; }
+    static __device__ __forceinline__ void st_f(S *p, R v, double, double) { *p = v; }
+    static __device__ __forceinline__ void st_g(S *p, R v, double, double) { *p = v; }
+};
+template <> struct Store<RBTP_STORE_F16S> {
+    using S = __half;
+    using R = float;
+    // w: lattice weight of the slot's direction, t0: reference temperature (g shift)
+    static __device__ __forceinline__ R ld_f(const S *p, double w, double) { return __half2float(*p) * (float)w; }
+    static __device__ __forceinline__ R ld_g(const S *p, double w, double t0)
+    {
+        return (__half2float(*p) + (float)t0) * (float)w;
+    }
+    static __device__ __forceinline__ void st_f(S *p, R v, double w, double)
+    {
+        *p = __float2half_rn(v * (float)(1.0 / w));
+    }
+    static __device__ __forceinline__ void st_g(S *p, R v, double w, double t0)
+    {
+        *p = __float2half_rn(v * (float)(1.0 / w) - (float)t0);
+    }
+};
+
+inline size_t store_bytes(int mode)
+{
+    return mode == RBTP_STORE_F64 ? 8 : (mode == RBTP_STORE_F32 ? 4 : 2);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Geometry and constants passed by value to kernels.
+// ------------------------------------------------------------------------------------------------
+struct Geo {
+    int lx, ly, lz;
+    long long lxy, L;
+};
+
+struct Phys {
+    double tau, tauc, grav0, beta, thot, tcold, t0, diff, visc, rho0;
+    double radius, mass, inertia, heat_cap, rho_ratio;
+    double rep_coeff, min_gap, min_gap_w, stf0, stf1, stf0_w, stf1_w;
+    double cp_ratio, vol_fraction;
+};
+
+// Device status word, read once per rbtp_step call.
+struct DevStatus {
+    int nonfinite;         // non-finite density seen by the step kernel
+    int link_overflow;     // a particle's link slab overflowed (bound violated)
+    int nf_overflow;       // new-fluid list overflowed
+    int contact_overflow;  // contact candidate list overflowed
+    int nf_count;          // new-fluid nodes of the last refill
+    int ncontacts;         // contact pairs of the last contact pass
+    int pad[2];
+};
+
+// Output selection of the step kernel.
+enum StepOut { OUT_NONE = 0, OUT_RHO = 1, OUT_MACROS = 2, OUT_MACROS_COL = 3 };
+
+// ------------------------------------------------------------------------------------------------
+// Kernel launch wrappers (defined in the .cu files).
+// ------------------------------------------------------------------------------------------------
+struct StepBuffers {
+    const void *fin, *gin;
+    void *fout, *gout;
+    double *faux;       // F_x of the previous step in, F_x of this step out (L)
+    double *rho_wall;   // density deviation at the x = 0 and x = LX-1 planes (2*LY*LZ)
+    double *rho, *ux, *uy, *uz, *phi;   // macro outputs (L each), may be null
+    double *fcol, *gcol;                // FP64 copy of the post-collision populations, may be null
+    DevStatus *status;
+};
+
+cudaError_t launch_step(int mode, bool pull, int out, const Geo &geo, const Phys &ph,
+                        const StepBuffers &b, cudaStream_t st);
+cudaError_t launch_stream_export(int mode, const Geo &geo, const Phys &ph, const void *fin,
+                                 const void *gin, const double *rho_wall, double *fout,
+                                 double *gout, cudaStream_t st);
+cudaError_t launch_home_export(int mode, const Geo &geo, const Phys &ph, const void *fin,
+                               const void *gin, double *fout, double *gout, cudaStream_t st);
+cudaError_t launch_home_import(int mode, const Geo &geo, const Phys &ph, const double *fin,
+                               const double *gin, void *fout, void *gout, cudaStream_t st);
+cudaError_t launch_fresh_init(int mode, const Geo &geo, const Phys &ph, void *f, void *g,
+                              double *faux, double *rho, double *ux, double *uy, double *uz,
+                              double *phi, cudaStream_t st);
+cudaError_t launch_macros_from_home(const Geo &geo, const double *f, const double *g, double *rho,
+                                    double *ux, double *uy, double *uz, double *phi,
+                                    cudaStream_t st);
+cudaError_t launch_forcing(const Geo &geo, const Phys &ph, const double *phi, double *faux,
+                           cudaStream_t st);
+
+// Particle pipeline ------------------------------------------------------------------------------
+struct PartBuffers {
+    int np;
+    double *state;          // 33 columns x np, column-major (col c at state + c*np)
+    double *hF, *hT, *hQ;   // hydrodynamic force, torque (3*np each), heat (np)
+    double *cF;             // contact force (3*np)
+    int *owner_cur, *owner_new;   // solid owner maps (L each); -1 = fluid
+    int link_cap;           // links per particle slab
+    int *link_node, *link_dir, *link_cnt;
+    double *link_q;
+    int nf_cap;
+    int *nf_node, *nf_pid;
+    double *nf_val;         // nf_cap * 54 refill values (27 f then 27 g)
+    double *nf_mac;         // nf_cap * 5 refill macros (rho, ux, uy, uz, phi)
+    // contacts
+    int ncell[3];
+    double cell_size;
+    int *cell_count, *cell_start, *cell_fill, *cell_items;
+    int cand_cap;
+    int pair_cap;
+    int *pair_p, *pair_q;
+    int box_half_mark, box_half_link, box_half_nf;
+};
+
+cudaError_t launch_links_ibb(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                             void *f, void *g, const double *rho, cudaStream_t st);
+cudaError_t launch_contacts(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                            DevStatus *status, cudaStream_t st);
+cudaError_t launch_update(const Phys &ph, const PartBuffers &pb, cudaStream_t st);
+cudaError_t launch_mark(const Geo &geo, const Phys &ph, const PartBuffers &pb, int *owner_out,
+                        cudaStream_t st);
+cudaError_t launch_link_fill(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                             const int *owner, DevStatus *status, cudaStream_t st);
+cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                          const int *owner_prev, const int *owner_cur, void *f, void *g,
+                          double *faux, const double *rho_wall, bool macros, double *rho,
+                          double *ux, double *uy, double *uz, double *phi, DevStatus *status,
+                          cudaStream_t st);
+cudaError_t launch_initial_owner(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                                 int *owner, cudaStream_t st);
+
+// Diagnostics ------------------------------------------------------------------------------------
+// Per-x-plane sums: 10 quantities x lx, see diagnostics.cu.
+constexpr int NPLANEQ = 10;
+cudaError_t launch_plane_sums(const Geo &geo, const Phys &ph, const double *ux, const double *uy,
+                              const double *uz, const double *phi, const int *owner,
+                              const double *pstate, int np, double *partials, int nchunks,
+                              double *plane, cudaStream_t st);
+cudaError_t launch_dissipation(const Geo &geo, const Phys &ph, const double *fcol,
+                               const double *gcol, const double *rho, const double *ux,
+                               const double *uy, const double *uz, const double *phi,
+                               const double *faux, const int *owner, double *ted, double *ked,
+                               cudaStream_t st);
+
+}  // namespace rbtp

@@ -1,0 +1,251 @@
+"""GPU parity of librbtp (called through its C ABI) against the CPU oracle.
+
+Tolerances (FP64 storage): populations and macroscopic fields within 1e-12 relative L2 after 100
+steps; integer structures (solid flags, owners, IBB link sets, new-fluid lists, contact pairs)
+bit-exact at identical particle states.  FP32/FP16 storage is compared with looser, stated
+tolerances.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from rbtp import Solver, RbtpError, STORE_F32, STORE_F16S, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+
+
+@pytest.fixture(scope="module")
+def env(lib_built, oracle_mod):
+    return oracle_mod
+
+
+def _pair(oracle_mod, cfg):
+    return Solver(cfg), oracle_mod.Oracle(cfg)
+
+
+def _compare_fields(s, o, tol=TOL64, macros=True):
+    fs, gs = s.fg()
+    fo, go = o.fg()
+    # f is in deviation form (values ~1e-3): compare against the population scale of g as well
+    assert rel_l2(gs, go) < tol, rel_l2(gs, go)
+    assert np.linalg.norm(fs - fo) / max(np.linalg.norm(go), 1e-300) < tol
+    if np.linalg.norm(fo) > 0:
+        assert rel_l2(fs, fo) < 1e3 * tol
+    if macros:
+        ms, mo = s.macros(), o.macros()
+        for k in ("rho", "ux", "uy", "uz", "phi", "force_x"):
+            scale = max(np.linalg.norm(mo[k]), np.linalg.norm(mo["phi"]) * 1e-3)
+            assert np.linalg.norm(ms[k] - mo[k]) / scale < tol, k
+
+
+def test_single_phase_fp64_100_steps(env):
+    cfg = W.config("plain_fp64")
+    s, o = _pair(env, cfg)
+    f, g, f7 = W.initial_state(cfg)
+    s.load_state(f, g, f7)
+    o.load_state(f, g, f7)
+    s.step(1, macros_last=True)
+    o.step(1)
+    _compare_fields(s, o, tol=1e-14)
+    s.step(99, macros_last=True)
+    o.step(99)
+    _compare_fields(s, o)
+    ns, no = np.array(s.nu(100)), np.array(o.nu(100))
+    assert np.allclose(ns, no, rtol=1e-10, atol=1e-12), (ns, no)
+    assert np.allclose(s.means(), o.means(), rtol=1e-9, atol=1e-15)
+    assert np.allclose(s.profile(), o.profile(), rtol=1e-9, atol=1e-15)
+    ts, ks = s.dissipation()
+    to, ko = o.dissipation()
+    assert rel_l2(ts, to) < 1e-10 and rel_l2(ks, ko) < 1e-10
+
+
+def test_fresh_init_fp64(env):
+    cfg = W.config("plain_fp64", lx=40, ly=24, lz=20)
+    s, o = _pair(env, cfg)
+    s.initialize()
+    o.initialize()
+    _compare_fields(s, o, tol=1e-15)
+    s.step(30, macros_last=True)
+    o.step(30)
+    _compare_fields(s, o)
+
+
+def test_size_independent_properties_fullsize_fp64(env):
+    # 320x320x160: exact mass conservation (bounce-back walls) and finite, bounded fields
+    cfg = W.config("production")
+    s = Solver(cfg)
+    f, g, f7 = W.initial_state(cfg)
+    s.load_state(f, g, f7)
+    s.step(10, macros_last=True)
+    fs, gs = s.fg()
+    assert abs(fs.sum()) < 1e-9
+    m = s.means()
+    assert np.all(np.isfinite(m)) and abs(m[3] - 0.5) < 1e-3
+    row = s.nu(10)
+    assert np.all(np.isfinite(row))
+
+
+@pytest.mark.parametrize("storage,tol_phi,tol_u", [(STORE_F32, 1e-6, 1e-3), (STORE_F16S, 2e-3, 0.3)])
+def test_reduced_storage_against_fp64(env, storage, tol_phi, tol_u):
+    cfg = W.config("plain_fp64", storage=storage)
+    s = Solver(cfg)
+    o = env.Oracle(W.config("plain_fp64"))
+    f, g, f7 = W.initial_state(cfg)
+    s.load_state(f, g, f7)
+    o.load_state(f, g, f7)
+    s.step(100, macros_last=True)
+    o.step(100)
+    ms, mo = s.macros(), o.macros()
+    assert rel_l2(ms["phi"], mo["phi"]) < tol_phi
+    assert rel_l2(ms["ux"], mo["ux"]) < tol_u
+    ns, no = s.nu(100), o.nu(100)
+    assert abs(ns[4] - no[4]) / abs(no[4]) < 10 * tol_phi  # Nu_bottom
+
+
+def _particle_cfg(**kw):
+    base = dict(lx=64, ly=64, lz=32, activate_particles=1, particle_diam_frac=8.0 / 64.0,
+                particle_fraction=0.02, rho_particle_ratio=1.0)
+    base.update(kw)
+    return W.config("plain_fp64", **base)
+
+
+def _links_equal(s, o):
+    a, b = s.links(), o.links()
+    assert len(a[0]) == len(b[0])
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a[3], b[3])  # q bit-exact
+
+
+def test_particles_init_and_links_bit_exact(env):
+    cfg = _particle_cfg()
+    s, o = _pair(env, cfg)
+    assert s.npart == o.npart == 9
+    s.initialize()
+    o.initialize()
+    assert np.array_equal(s.particles(), o.particles())   # glibc rand placement, pinit.cu:97-144
+    assert np.array_equal(s.flags(), o.flags())
+    _links_equal(s, o)
+    _compare_fields(s, o, tol=1e-15)
+
+
+def test_particles_fp64_100_steps(env):
+    cfg = _particle_cfg()
+    s, o = _pair(env, cfg)
+    s.initialize()
+    o.initialize()
+    f, g, f7 = W.initial_state(cfg)
+    p = o.particles()
+    s.load_state(f, g, f7, p)
+    o.load_state(f, g, f7, p)
+    s.step(1, macros_last=True)
+    o.step(1)
+    _compare_fields(s, o, tol=1e-13)
+    ps, po = s.particles(), o.particles()
+    assert np.abs(ps - po).max() <= 1e-12 * max(1.0, np.abs(po).max())
+    assert np.array_equal(s.flags(), o.flags())
+    s.step(99, macros_last=True)
+    o.step(99)
+    _compare_fields(s, o)
+    ps, po = s.particles(), o.particles()
+    scale = np.maximum(np.abs(po).max(0), 1e-300)
+    assert np.all(np.abs(ps - po).max(0) <= 1e-10 * scale + 1e-16)
+    assert np.array_equal(s.flags(), o.flags())
+    ns, no = np.array(s.nu(100)), np.array(o.nu(100))
+    assert np.allclose(ns, no, rtol=1e-9, atol=1e-12)
+
+
+def test_links_contacts_new_fluid_bit_exact_at_identical_state(env):
+    # hand-placed spheres: two pairs inside the contact range, one near a wall
+    cfg = _particle_cfg(particle_fraction=0.01)
+    s, o = _pair(env, cfg)
+    n = s.npart
+    assert n >= 4
+    rng = np.random.default_rng(7)
+    p = np.zeros((n, 33))
+    p[:, 30] = 0.5
+    base = [(20.3, 20.1, 16.2), (28.9, 20.6, 16.0), (40.2, 40.7, 12.3), (40.9, 48.6, 13.1)]
+    for k in range(n):
+        if k < len(base):
+            p[k, :3] = base[k]
+        else:
+            p[k, :3] = [10 + 44 * rng.random(), 8 + 48 * rng.random(), 6 + 20 * rng.random()]
+    p[:, 3:6] = 0.02 * rng.standard_normal((n, 3))
+    p[:, 18:21] = 0.002 * rng.standard_normal((n, 3))
+    f, g, f7 = W.initial_state(cfg)
+    s.load_state(f, g, f7, p)
+    o.load_state(f, g, f7, p)
+    assert np.array_equal(s.flags(), o.flags())
+    _links_equal(s, o)
+    s.step(1)
+    o.step(1)
+    cs, co = s.contacts(), o.contacts()
+    assert len(cs[0]) >= 2
+    assert np.array_equal(cs[0], co[0]) and np.array_equal(cs[1], co[1])
+    # contact forces are summed in the same (ascending partner) order: bit-exact history columns
+    ps, po = s.particles(), o.particles()
+    # force_prev holds last step's total; this step's contact part is inside force (col 6-8)
+    assert np.array_equal(s.flags(), o.flags())
+    nfs, nfo = s.new_fluid(), o.new_fluid()
+    assert np.array_equal(nfs[0], nfo[0]) and np.array_equal(nfs[1], nfo[1])
+    # identical particle state -> identical links
+    s.load_state(*s.fg(), None, ps)
+    o.load_state(*s.fg(), None, ps)
+    assert np.array_equal(s.flags(), o.flags())
+    _links_equal(s, o)
+
+
+def test_gpu_is_deterministic(env):
+    cfg = _particle_cfg()
+    outs = []
+    for _ in range(2):
+        s = Solver(cfg)
+        s.initialize()
+        s.step(20, macros_last=True)
+        outs.append((s.fg(), s.particles(), s.nu(20)))
+        s.close()
+    (f1, g1), p1, n1 = outs[0]
+    (f2, g2), p2, n2 = outs[1]
+    assert np.array_equal(f1, f2) and np.array_equal(g1, g2)
+    assert np.array_equal(p1, p2) and n1 == n2
+
+
+def test_nonfinite_watchdog(env):
+    cfg = W.config("plain_fp64", lx=16, ly=16, lz=8)
+    s = Solver(cfg)
+    f, g, f7 = W.initial_state(cfg)
+    g = g.copy()
+    g[12345 % g.size] = np.nan
+    s.load_state(f, g, f7)
+    with pytest.raises(RbtpError) as e:
+        s.step(2)
+    assert e.value.status == -4
+
+
+def test_restart_files_roundtrip(env, tmp_path):
+    cfg = W.config("plain_fp64", lx=32, ly=24, lz=16, nflowout=10)
+    s = Solver(cfg)
+    f, g, f7 = W.initial_state(cfg)
+    s.load_state(f, g, f7)
+    s.step(10)
+    d = str(tmp_path)
+    s.output_flow(10, d)
+    s.output_fg(10, d)
+    r = Solver(cfg)
+    r.load_restart(d, 10)
+    assert r.istep == 10
+    s.step(7, macros_last=True)
+    r.step(7, macros_last=True)
+    fa, ga = s.fg()
+    fb, gb = r.fg()
+    assert np.array_equal(fa, fb) and np.array_equal(ga, gb)
+    # a truncated restart file is rejected with an error status, not an exit
+    with open(tmp_path / "fg000000010.dat", "r+b") as fh:
+        fh.truncate(1000)
+    with pytest.raises(RbtpError) as e:
+        Solver(cfg).load_restart(d, 10)
+    assert e.value.status == -6
