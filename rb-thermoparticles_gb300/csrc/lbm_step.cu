@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(128) k_step(const Geo geo, const Phys ph, cons
             // x exit takes the Dirichlet anti-bounce-back with the node's density deviation.
             if (ox && !oy && !oz) {
                 const double tw = (cx == 1) ? ph.thot : ph.tcold;
-                gr = (R)(-(double)gr + 2.0 * w * tw * (1.0 + rw));
+                gr = (R)wall_image((double)gr, w, tw, rw);
             }
             g[i] = gr;
         }
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(128) k_stream_export(const Geo geo, const Phys
         double gr = (double)ST::ld_g(gin + src, w, ph.t0);
         if (ox && !oy && !oz) {
             const double tw = (cx == 1) ? ph.thot : ph.tcold;
-            gr = -gr + 2.0 * w * tw * (1.0 + rw);
+            gr = wall_image(gr, w, tw, rw);
         }
         gout[(long long)i * L + node] = gr;
     });

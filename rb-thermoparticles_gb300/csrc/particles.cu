@@ -729,7 +729,7 @@ __global__ void k_refill_scatter(const Geo geo, const Phys ph, const PartBuffers
                 // the pull applies g <- -stored + 2 w T_wall (1 + rho_wall); store its preimage
                 const double tw = (cx == 1) ? ph.thot : ph.tcold;
                 const long long ws = (long long)iz * geo.ly + iy + (cx == 1 ? 0 : (long long)geo.lz * geo.ly);
-                gs = 2.0 * w * tw * (1.0 + rho_wall[ws]) - gv;
+                gs = wall_image(gv, w, tw, rho_wall[ws]);
             }
             ST::st_g(gB + (long long)o * L + idx, (R)gs, w, ph.t0);
         }

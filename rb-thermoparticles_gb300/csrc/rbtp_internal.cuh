@@ -118,6 +118,13 @@ template <> struct Store<RBTP_STORE_F16S> {
     }
 };
 
+// Dirichlet anti-bounce-back image of streaming.cu:55-60, g_i = -g_opp + 2 w_i T_wall (1 + rho),
+// rounded the same way (one fused multiply-add) in every kernel that applies or inverts it.
+__device__ __forceinline__ double wall_image(double g, double w, double t_wall, double rho)
+{
+    return __fma_rn(__dmul_rn(2.0 * w, t_wall), __dadd_rn(1.0, rho), -g);
+}
+
 inline size_t store_bytes(int mode)
 {
     return mode == RBTP_STORE_F64 ? 8 : (mode == RBTP_STORE_F32 ? 4 : 2);
