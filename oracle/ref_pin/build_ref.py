@@ -1,0 +1,64 @@
+#!/usr/bin/env python3
+"""Compile the reference's own device code, per pin case, into oracle/_ref/<case>.cubin.
+
+TEST INFRASTRUCTURE ONLY.  Reads the reference sources where they lie (/root/reference, present only
+on the development machine), compiles them with nvcc for sm_103a (-rdc, the reference's
+-std=c++14 raised to c++17 because CUDA 13's headers require it) against a generated parameters.h,
+and device-links the objects into one cubin.  Nothing is copied from the reference: outputs go to
+oracle/_ref/ only (git-ignored), and the cubin travels to GPU hosts as a build artefact.  The host
+half of the reference (main.cu's loop, the particle wrappers) is restated by ref_driver.cpp.
+"""
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import cases  # noqa: E402
+
+REF = "/root/reference"
+OUT = os.path.join(os.path.dirname(HERE), "_ref")
+SOURCES = ["src_lbm/globals.cu", "src_lbm/initial.cu", "src_lbm/collision.cu", "src_lbm/streaming.cu",
+           "src_lbm/macrovar.cu", "src_part/pinit.cu", "src_part/links.cu", "src_part/refill.cu",
+           "src_part/ibb.cu", "src_part/pforces.cu", "src_part/move.cu"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def build_case(case: str) -> str:
+    cdir = os.path.join(OUT, case)
+    os.makedirs(os.path.join(cdir, "obj"), exist_ok=True)
+    with open(os.path.join(cdir, "parameters.h"), "w") as fh:
+        fh.write(cases.parameters_h(case))
+    cubin = os.path.join(OUT, case + ".cubin")
+    objs = []
+    cmds = []
+    for src in SOURCES:
+        o = os.path.join(cdir, "obj", src.replace("/", "_").replace(".cu", ".o"))
+        objs.append(o)
+        cmds.append(["nvcc"] + ARCH + ["-O3", "-std=c++17", "-rdc=true", "-I" + cdir,
+                                       "-I" + os.path.join(REF, "include"), "-I" + REF,
+                                       "-c", os.path.join(REF, src), "-o", o])
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        for r in ex.map(lambda c: subprocess.run(c, capture_output=True, text=True), cmds):
+            if r.returncode != 0:
+                raise RuntimeError("reference compile failed:\n" + r.stdout + r.stderr)
+    r = subprocess.run(["nvcc"] + ARCH + ["-dlink", "-cubin", "-o", cubin] + objs, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("device link failed:\n" + r.stdout + r.stderr)
+    for o in objs:  # host objects are not needed past the device link
+        os.remove(o)
+    return cubin
+
+
+def main() -> int:
+    if not os.path.isdir(REF):
+        print("reference sources not present; nothing to build")
+        return 0
+    for case in cases.CASES:
+        print("built", build_case(case))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

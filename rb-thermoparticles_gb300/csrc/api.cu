@@ -264,6 +264,8 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
     ph.min_gap = cfg->rep_min_gap; ph.min_gap_w = cfg->rep_min_gap_w;
     ph.stf0 = cfg->rep_stf0; ph.stf1 = cfg->rep_stf1; ph.stf0_w = cfg->rep_stf0_w; ph.stf1_w = cfg->rep_stf1_w;
     ph.cp_ratio = cfg->cp_particle_ratio; ph.vol_fraction = cfg->particle_fraction;
+    ph.kd = make_step_consts<double>(ph);
+    ph.kf = make_step_consts<float>(ph);
 
     auto cleanup_fail = [&](int code) { rbtp_destroy(h); return code; };
 #define CKC(call)                                                                    \

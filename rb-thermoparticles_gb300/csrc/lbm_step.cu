@@ -27,8 +27,18 @@ struct NodeIdx {
     long long node;
 };
 
+// Resident 128-thread blocks per SM requested from the register allocator (FP64 is bound by the
+// FP64 pipe, the FP32/FP16 storage modes by HBM bandwidth).
+#ifndef RBTP_STEP_MINB_F64
+#define RBTP_STEP_MINB_F64 1
+#endif
+#ifndef RBTP_STEP_MINB_LOW
+#define RBTP_STEP_MINB_LOW 1
+#endif
+
 template <int MODE, bool PULL, int OUT>
-__global__ void __launch_bounds__(128) k_step(const Geo geo, const Phys ph, const StepBuffers b)
+__global__ void __launch_bounds__(128, MODE == RBTP_STORE_F64 ? RBTP_STEP_MINB_F64 : RBTP_STEP_MINB_LOW)
+    k_step(const Geo geo, const Phys ph, const StepBuffers b)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
@@ -44,13 +54,11 @@ __global__ void __launch_bounds__(128) k_step(const Geo geo, const Phys ph, cons
     S *__restrict__ fout = static_cast<S *>(b.fout);
     S *__restrict__ gout = static_cast<S *>(b.gout);
     const double t0 = ph.t0;
-
     const bool xlo = ix == 0, xhi = ix == geo.lx - 1;
     const bool ylo = iy == 0, yhi = iy == geo.ly - 1;
     const bool zlo = iz == 0, zhi = iz == geo.lz - 1;
     const long long wall_slot = (long long)iz * geo.ly + iy;
-    double rw = 0.0;
-    if (PULL && (xlo || xhi)) rw = b.rho_wall[(xhi ? (long long)geo.lz * geo.ly : 0) + wall_slot];
+    const StepK<R> &K = step_consts<R>(ph);
 
     R f[27], g[27];
     unroll<27>([&](auto I) {
@@ -61,29 +69,39 @@ __global__ void __launch_bounds__(128) k_step(const Geo geo, const Phys ph, cons
             f[i] = ST::ld_f(fin + (long long)i * L + node, w, t0);
             g[i] = ST::ld_g(gin + (long long)i * L + node, w, t0);
         } else {
-            const bool ox = (cx == 1 && xlo) || (cx == -1 && xhi);
-            const bool oy = (cy == 1 && ylo) || (cy == -1 && yhi);
-            const bool oz = (cz == 1 && zlo) || (cz == -1 && zhi);
-            const bool out = ox || oy || oz;
+            // f_i(x) = f*_i(x - c_i); a neighbour outside the box returns f*_opp(x) (bounce-back)
+            const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
+                             (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
             const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
             const long long src = out ? ((long long)o * L + node) : ((long long)i * L + node - off);
             f[i] = ST::ld_f(fin + src, w, t0);
-            R gr = ST::ld_g(gin + src, w, t0);
-            // streaming.cu:45-61: a z or y exit is adiabatic even at the x walls; only a pure
-            // x exit takes the Dirichlet anti-bounce-back with the node's density deviation.
-            if (ox && !oy && !oz) {
-                const double tw = (cx == 1) ? ph.thot : ph.tcold;
-                gr = (R)wall_image((double)gr, w, tw, rw);
-            }
-            g[i] = gr;
+            g[i] = ST::ld_g(gin + src, w, t0);
         }
     });
+    if constexpr (PULL) {
+        // streaming.cu:45-61: at the x walls a direction that leaves only through x takes the
+        // Dirichlet anti-bounce-back with the node's density deviation of the previous step; y/z
+        // exits stay adiabatic.  Only warps holding x-wall nodes enter this branch.
+        if (xlo || xhi) {
+            const R rw = (R)b.rho_wall[(xhi ? (long long)geo.lz * geo.ly : 0) + wall_slot];
+            const R tw = xlo ? K.thot : K.tcold;
+            unroll<27>([&](auto I) {
+                constexpr int i = decltype(I)::value;
+                constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+                if constexpr (cx != 0) {
+                    const bool ox = (cx == 1) ? xlo : xhi;
+                    const bool oyz = (cy == 1 && ylo) || (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
+                    if (ox && !oyz) g[i] = wall_image(g[i], dweight(i), tw, rw);
+                }
+            });
+        }
+    }
 
     // ---- moments (macrovar.cu:3-34), pairwise ----
     R rho = f[0], jx = 0, jy = 0, jz = 0;
     R phi = g[0], kx = 0, ky = 0, kz = 0;
-    unroll<13>([&](auto K) {
-        constexpr int i = dpair(decltype(K)::value);
+    unroll<13>([&](auto Kp) {
+        constexpr int i = dpair(decltype(Kp)::value);
         constexpr int o = dopp(i);
         constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
         const R sf = f[i] + f[o], df = f[i] - f[o];
@@ -97,12 +115,12 @@ __global__ void __launch_bounds__(128) k_step(const Geo geo, const Phys ph, cons
         if constexpr (cz == 1) { jz += df; kz += dg; }
         if constexpr (cz == -1) { jz -= df; kz -= dg; }
     });
-    if (!(fabs((double)rho) < 1e30) || !(fabs((double)phi) < 1e30)) atomicOr(&b.status->nonfinite, 1);
+    if (!(fabs(rho) < (R)1e30) || !(fabs(phi) < (R)1e30)) atomicOr(&b.status->nonfinite, 1);
 
-    const double fold = b.faux[node];
-    const R ux = jx + (R)(0.5 * fold), uy = jy, uz = jz;
+    const R fold = (R)b.faux[node];
+    const R ux = jx + (R)0.5 * fold, uy = jy, uz = jz;
     // forcing (macrovar.cu:45): F_x = g0 beta (phi - T0); F_y = F_z = 0 always
-    const R Fx = (R)(ph.grav0 * ph.beta) * (phi - (R)t0);
+    const R Fx = K.g0b * (phi - K.t0);
     b.faux[node] = (double)Fx;
 
     if constexpr (OUT >= OUT_MACROS) {
@@ -118,55 +136,67 @@ __global__ void __launch_bounds__(128) k_step(const Geo geo, const Phys ph, cons
     if (xhi) b.rho_wall[(long long)geo.lz * geo.ly + wall_slot] = (double)rho;
 
     // ---- f collision (collision.cu:3-33) ----
-    const R tinv = (R)(1.0 / ph.tau);
-    const R om = (R)(1.0 - 1.0 / ph.tau);
-    const R G = (R)(3.0 * (1.0 - 0.5 / ph.tau)) * Fx;
+    // f*_i = om f_i + w_i [ (rho + P_i)/tau + G (c_ix - u_x)(1 + P_i) ],  P_i = A_i + B_i,
+    // A = 4.5 (c.u)^2 - 1.5 u^2, B = 3 c.u, G = 3 (1 - 1/(2 tau)) F_x.
+    const R G = K.Gc * Fx;
     const R Gux = G * ux;
     const R h = (R)1.5 * (ux * ux + uy * uy + uz * uz);
-    const R k1 = tinv - Gux;
-    const R k0 = rho * tinv - Gux;
+    const R k1 = K.tinv - Gux;
+    const R k0 = rho * K.tinv - Gux;
     // ---- g collision (collision.cu:35-89) ----
-    const R tcinv = (R)(1.0 / ph.tauc);
-    const R omc = (R)(1.0 - 1.0 / ph.tauc);
-    const R gd = rho / (R)3 + (R)(2.0 * ph.tauc / 3.0);
+    // g*_i = omc g_i + geqnew_i / tauc + w_i c_i.V, with the source vector
+    // V = Rc [ -2 rho/gd (sum_i c_i g_i - phi u) + x F_x phi (3 - rho/gd) ],  gd = rho/3 + 2 tauc/3.
+    const R gd = rho * (R)(1.0 / 3.0) + K.gd0;
     const R rgd = rho / gd;
-    const R Rc = (R)(1.0 - 1.0 / (2.0 * ph.tauc));
-    const R c2 = (R)(-2) * rgd * Rc;
-    const R Vx = c2 * (kx - phi * ux) + Rc * Fx * phi * ((R)3 - rgd);
+    const R c2 = (R)(-2) * rgd * K.Rc;
+    const R Vx = c2 * (kx - phi * ux) + K.Rc * Fx * phi * ((R)3 - rgd);
     const R Vy = c2 * (ky - phi * uy);
     const R Vz = c2 * (kz - phi * uz);
-    const R pt = phi * tcinv;
+    const R pt = phi * K.tcinv;
     const R ptb = pt * ((R)1 + rho);
 
     {
         constexpr R w0 = (R)dweight(0);
-        f[0] = om * f[0] + w0 * (k0 - h * k1);
-        g[0] = omc * g[0] + (w0 * (ptb - pt * h) - pt * rho);
+        f[0] = K.om * f[0] + w0 * (k0 - h * k1);
+        g[0] = K.omc * g[0] + (w0 * (ptb - pt * h) - pt * rho);
     }
-    unroll<13>([&](auto K) {
-        constexpr int i = dpair(decltype(K)::value);
-        constexpr int o = dopp(i);
-        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
-        constexpr R w = (R)dweight(i);
-        R cu = 0, cV = 0;
-        if constexpr (cx != 0) { cu += (R)cx * ux; cV += (R)cx * Vx; }
-        if constexpr (cy != 0) { cu += (R)cy * uy; cV += (R)cy * Vy; }
-        if constexpr (cz != 0) { cu += (R)cz * uz; cV += (R)cz * Vz; }
-        const R A = (R)4.5 * cu * cu - h;
-        const R B = (R)3 * cu;
-        R fS = A * k1 + k0;
-        R fD = B * k1;
-        if constexpr (cx != 0) {
-            fS += (R)cx * (G * B);
-            fD += (R)cx * (G + G * A);
-        }
-        const R gS = A * pt + ptb;
-        const R gD = B * pt + cV;
-        const R fi = f[i], fo = f[o], gi = g[i], go = g[o];
-        f[i] = om * fi + w * (fS + fD);
-        f[o] = om * fo + w * (fS - fD);
-        g[i] = omc * gi + w * (gS + gD);
-        g[o] = omc * go + w * (gS - gD);
+    // Pairs grouped by weight class (face, edge, corner); the class constants fold w_i into the
+    // per-node coefficients and live only while their class is processed.
+    unroll<3>([&](auto C) {
+        constexpr int c = decltype(C)::value + 1;
+        constexpr R w = (R)(c == 1 ? 2.0 / 27.0 : (c == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
+        const R wk1 = w * k1;
+        const R ca = (R)4.5 * wk1, cb = w * k0 - h * wk1, c3 = (R)3 * wk1;
+        const R wG = w * G;
+        const R ce = (R)4.5 * wG, cd = wG - h * wG, cg = (R)3 * wG;
+        const R wpt = w * pt;
+        const R ga = (R)4.5 * wpt, gb = w * ptb - h * wpt, gc = (R)3 * wpt;
+        const R vx = w * Vx, vy = w * Vy, vz = w * Vz;
+        unroll<13>([&](auto Kp) {
+            constexpr int i = dpair(decltype(Kp)::value);
+            if constexpr (dclass(i) == c) {
+                constexpr int o = dopp(i);
+                constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+                R cu = 0, cV = 0;
+                if constexpr (cx != 0) { cu += (R)cx * ux; cV += (R)cx * vx; }
+                if constexpr (cy != 0) { cu += (R)cy * uy; cV += (R)cy * vy; }
+                if constexpr (cz != 0) { cu += (R)cz * uz; cV += (R)cz * vz; }
+                const R q = cu * cu;
+                R wS = q * ca + cb;                 // w (A k1 + k0)
+                R wD = cu * c3;                     // w B k1
+                if constexpr (cx != 0) {
+                    wS += (R)cx * (cu * cg);        // w cx G B
+                    wD += (R)cx * (q * ce + cd);    // w cx G (1 + A)
+                }
+                const R gS = q * ga + gb;           // w pt (1 + rho + A)
+                const R gD = cu * gc + cV;          // w pt B + w c.V
+                const R fi = f[i], fo = f[o], gi = g[i], go = g[o];
+                f[i] = K.om * fi + (wS + wD);
+                f[o] = K.om * fo + (wS - wD);
+                g[i] = K.omc * gi + (gS + gD);
+                g[o] = K.omc * go + (gS - gD);
+            }
+        });
     });
 
     unroll<27>([&](auto I) {

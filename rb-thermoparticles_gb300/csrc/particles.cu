@@ -447,15 +447,44 @@ __global__ void k_mark(const Geo geo, const Phys ph, const PartBuffers pb, int *
 
 // ------------------------------------------------------------------------------------------------
 // Link slabs (links.cu:50-139): CTA per particle, ordered compaction over its padded box.
+// Phase 1 (integer work only): every fluid node of the box within r + 2 of the centre marks the
+// directions whose neighbour this particle owns; the candidates (node, direction) are compacted in
+// node-then-direction order into shared memory.  Phase 2: the FP64 ray-sphere q of links.cu:7-23
+// runs over the compacted candidates with all lanes busy, and accepted links are appended to the
+// particle's slab in the same order.
 // ------------------------------------------------------------------------------------------------
 constexpr int LINK_THREADS = 256;
+constexpr int LINK_CAND = LINK_THREADS * 26;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += t;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    int wbase = 0, tot = 0;
+#pragma unroll
+    for (int k = 0; k < LINK_THREADS / 32; ++k) {
+        const int s = wsum[k];
+        if (k < warp) wbase += s;
+        tot += s;
+    }
+    __syncthreads();
+    total = tot;
+    return wbase + incl - v;
+}
 
 __global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const Phys ph,
                                                             const PartBuffers pb, const int *owner,
                                                             DevStatus *status)
 {
     __shared__ int wsum[LINK_THREADS / 32];
-    __shared__ int base_sh;
+    __shared__ int cand[LINK_CAND];  // (box-local node index << 5) | direction
     const int p = blockIdx.x;
     const double *st = pb.state;
     const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
@@ -463,82 +492,80 @@ __global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const
     const double rsq = dmul(r, r);
     const Box b = sphere_box(geo, px, py, pz, r, 1);
     const long long slab = (long long)p * pb.link_cap;
-    if (threadIdx.x == 0) base_sh = 0;
-    __syncthreads();
     if (b.x0 > b.x1 || b.y0 > b.y1 || b.z0 > b.z1) {
         if (threadIdx.x == 0) pb.link_cnt[p] = 0;
         return;
     }
     const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
     const int total = nx * ny * nz;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // conservative single-precision shell test: a link needs |x - X| <= r + sqrt(3)
+    const float reach = (float)r + 2.0f;
+    const float reach2 = reach * reach;
+    int base = 0;
     for (int c0 = 0; c0 < total; c0 += LINK_THREADS) {
         const int t = c0 + threadIdx.x;
         unsigned mask = 0;
-        int ix = 0, iy = 0, iz = 0;
-        double qv[26];
         if (t < total) {
             const int lz = t / (nx * ny);
             const int rem = t - lz * nx * ny;
             const int ly = rem / nx;
-            ix = b.x0 + (rem - ly * nx); iy = b.y0 + ly; iz = b.z0 + lz;
+            const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
+            const float ddx = (float)((double)ix + 0.5 - px), ddy = (float)((double)iy + 0.5 - py),
+                        ddz = (float)((double)iz + 0.5 - pz);
             const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
-            if (owner[idx] < 0) {
-                const double x0 = (double)ix + 0.5, y0 = (double)iy + 0.5, z0 = (double)iz + 0.5;
+            if (ddx * ddx + ddy * ddy + ddz * ddz <= reach2 && owner[idx] < 0) {
                 unroll<26>([&](auto K) {
                     constexpr int ip = decltype(K)::value + 1;
                     constexpr int cx = dcx(ip), cy = dcy(ip), cz = dcz(ip);
                     const int xn = ix + cx, yn = iy + cy, zn = iz + cz;
                     if (xn >= 0 && xn < geo.lx && yn >= 0 && yn < geo.ly && zn >= 0 && zn < geo.lz) {
-                        const long long nidx = (long long)zn * geo.lxy + (long long)yn * geo.lx + xn;
-                        if (owner[nidx] == p) {
-                            double q;
-                            if (link_q(cx, cy, cz, x0, y0, z0, px, py, pz, rsq, q)) {
-                                mask |= 1u << (ip - 1);
-                                qv[ip - 1] = q;
-                            }
-                        }
+                        const long long nidx = idx + cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
+                        if (owner[nidx] == p) mask |= 1u << ip;
                     }
                 });
             }
         }
-        const int cnt = __popc(mask);
-        // block exclusive scan of cnt in thread order (= node index order)
-        int incl = cnt;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, off);
-            if (lane >= off) incl += v;
+        int ccount;
+        int pos = block_exclusive_scan(__popc(mask), wsum, ccount);
+        while (mask) {
+            const int ip = __ffs(mask) - 1;
+            mask &= mask - 1;
+            cand[pos++] = (t << 5) | ip;
         }
-        if (lane == 31) wsum[warp] = incl;
         __syncthreads();
-        int wbase = 0, ctotal = 0;
-        for (int k = 0; k < LINK_THREADS / 32; ++k) {
-            if (k < warp) wbase += wsum[k];
-            ctotal += wsum[k];
-        }
-        int pos = base_sh + wbase + incl - cnt;
-        if (mask) {
-            const long long node = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
-            unroll<26>([&](auto K) {
-                constexpr int ip = decltype(K)::value + 1;
-                if (mask & (1u << (ip - 1))) {
-                    if (pos < pb.link_cap) {
-                        pb.link_node[slab + pos] = (int)node;
-                        pb.link_dir[slab + pos] = ip;
-                        pb.link_q[slab + pos] = qv[ip - 1];
-                    } else {
-                        atomicOr(&status->link_overflow, 1);
-                    }
-                    ++pos;
+        // phase 2: q for the compacted candidates, order-preserving append
+        for (int k0 = 0; k0 < ccount; k0 += LINK_THREADS) {
+            const int k = k0 + threadIdx.x;
+            int ok = 0, node = 0, ip = 0;
+            double q = 0.0;
+            if (k < ccount) {
+                const int cv = cand[k];
+                const int tt = cv >> 5;
+                ip = cv & 31;
+                const int lz = tt / (nx * ny);
+                const int rem = tt - lz * nx * ny;
+                const int ly = rem / nx;
+                const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
+                node = (int)((long long)iz * geo.lxy + (long long)iy * geo.lx + ix);
+                ok = link_q(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (double)ix + 0.5, (double)iy + 0.5,
+                            (double)iz + 0.5, px, py, pz, rsq, q) ? 1 : 0;
+            }
+            int ltotal;
+            const int lpos = base + block_exclusive_scan(ok, wsum, ltotal);
+            if (ok) {
+                if (lpos < pb.link_cap) {
+                    pb.link_node[slab + lpos] = node;
+                    pb.link_dir[slab + lpos] = ip;
+                    pb.link_q[slab + lpos] = q;
+                } else {
+                    atomicOr(&status->link_overflow, 1);
                 }
-            });
+            }
+            base += ltotal;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) base_sh += ctotal;
         __syncthreads();
     }
-    if (threadIdx.x == 0) pb.link_cnt[p] = base_sh;
+    if (threadIdx.x == 0) pb.link_cnt[p] = base;
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -124,6 +124,11 @@ __device__ __forceinline__ double wall_image(double g, double w, double t_wall, 
 {
     return __fma_rn(__dmul_rn(2.0 * w, t_wall), __dadd_rn(1.0, rho), -g);
 }
+__device__ __forceinline__ float wall_image(float g, double w, float t_wall, float rho)
+{
+    return __fmaf_rn(__fmul_rn((float)(2.0 * w), t_wall), __fadd_rn(1.0f, rho), -g);
+}
+
 
 inline size_t store_bytes(int mode)
 {
@@ -138,12 +143,51 @@ struct Geo {
     long long lxy, L;
 };
 
+// Relaxation and forcing constants of the step kernel, precomputed on the host in the kernel's
+// arithmetic type (per-thread double divisions would occupy GB300's narrow FP64 pipe).
+template <class R>
+struct StepK {
+    R tinv, om;        // 1/tau, 1 - 1/tau                    (collision.cu:17-18,27)
+    R Gc;              // 3 (1 - 1/(2 tau)): Guo force factor  (collision.cu:18,28-30)
+    R tcinv, omc;      // 1/tauc, 1 - 1/tauc                  (collision.cu:85-86)
+    R gd0, Rc;         // 2 tauc / 3, 1 - 1/(2 tauc)          (collision.cu:72-73)
+    R g0b, t0;         // grav0 * beta, T_REF                 (macrovar.cu:45)
+    R thot, tcold;     // wall temperatures                   (streaming.cu:55-58)
+};
+
 struct Phys {
     double tau, tauc, grav0, beta, thot, tcold, t0, diff, visc, rho0;
+    StepK<double> kd;
+    StepK<float> kf;
     double radius, mass, inertia, heat_cap, rho_ratio;
     double rep_coeff, min_gap, min_gap_w, stf0, stf1, stf0_w, stf1_w;
     double cp_ratio, vol_fraction;
 };
+
+template <class R>
+__host__ __device__ __forceinline__ const StepK<R> &step_consts(const Phys &ph)
+{
+    if constexpr (sizeof(R) == 8) return ph.kd;
+    else return ph.kf;
+}
+
+template <class R>
+inline StepK<R> make_step_consts(const Phys &ph)
+{
+    StepK<R> k;
+    k.tinv = (R)(1.0 / ph.tau);
+    k.om = (R)(1.0 - 1.0 / ph.tau);
+    k.Gc = (R)(3.0 * (1.0 - 0.5 / ph.tau));
+    k.tcinv = (R)(1.0 / ph.tauc);
+    k.omc = (R)(1.0 - 1.0 / ph.tauc);
+    k.gd0 = (R)(2.0 * ph.tauc / 3.0);
+    k.Rc = (R)(1.0 - 1.0 / (2.0 * ph.tauc));
+    k.g0b = (R)(ph.grav0 * ph.beta);
+    k.t0 = (R)ph.t0;
+    k.thot = (R)ph.thot;
+    k.tcold = (R)ph.tcold;
+    return k;
+}
 
 // Device status word, read once per rbtp_step call.
 struct DevStatus {

