@@ -19,7 +19,10 @@ import cases  # noqa: E402
 
 REF = "/root/reference"
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
-SOURCES = ["src_lbm/globals.cu", "src_lbm/initial.cu", "src_lbm/collision.cu", "src_lbm/streaming.cu",
+# main.cu and output/*.cu launch macrovar/collision/streaming and compute_Ked/ted; compiling them
+# keeps those kernels referenced so the device link does not discard them.
+SOURCES = ["main.cu", "output/output_flow.cu", "output/output_statis.cu", "output/output_part.cu",
+           "src_lbm/globals.cu", "src_lbm/initial.cu", "src_lbm/collision.cu", "src_lbm/streaming.cu",
            "src_lbm/macrovar.cu", "src_part/pinit.cu", "src_part/links.cu", "src_part/refill.cu",
            "src_part/ibb.cu", "src_part/pforces.cu", "src_part/move.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -33,7 +33,7 @@ struct NodeIdx {
 #define RBTP_STEP_MINB_F64 1
 #endif
 #ifndef RBTP_STEP_MINB_LOW
-#define RBTP_STEP_MINB_LOW 1
+#define RBTP_STEP_MINB_LOW 6  // 6 x 128 threads (<= 80 registers): best of a 1/5/6/8 sweep on GB300
 #endif
 
 template <int MODE, bool PULL, int OUT>
