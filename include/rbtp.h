@@ -196,6 +196,26 @@ int  rbtp_write_flow(rbtp_handle *h, const char *dir, int istep);        /* outp
 int  rbtp_write_fg(rbtp_handle *h, const char *dir, int istep);          /* output_fg     */
 int  rbtp_write_particles(rbtp_handle *h, const char *dir, int istep);   /* output_particles */
 
+/* ---- allocation-free diagnostic sums ----------------------------------------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device memory — code hosted in
+ * a framework that owns the whole device memory pool, or a loop that cannot afford the implicit
+ * device synchronisation of cudaMalloc/cudaFree.  Computes, on the caller's stream, the ten per-x-
+ * plane sums behind rbtp_nu / rbtp_means / rbtp_profile (layout [10][lx]: fluid sum of ux*phi,
+ * fluid count, solid sum of ux*phi, solid count, wall-Nusselt sum, wall count, then the sums of
+ * ux, uy, uz, phi with solid nodes taken at the rigid-body velocity and particle temperature) from
+ * device arrays the caller owns: ux, uy, uz, phi (L doubles each), owner (L ints, -1 = fluid; NULL
+ * = no particles), particle_state (npart x RBTP_PARTICLE_COLS doubles, column-major: column c at
+ * particle_state + c*npart), plane_sums (10*lx doubles, written).  It calls no allocator: its
+ * partial sums live in one fixed device array of RBTP_NOALLOC_MAX_LX planes (2.6 MB per GPU, kept
+ * until the process exits) whose address is looked up on the first call on each device, so make
+ * that first call before any stream capture.  Calls share that array: calls that overlap on the GPU
+ * race.  lx > RBTP_NOALLOC_MAX_LX returns RBTP_ERR_CAPACITY. */
+#define RBTP_NOALLOC_MAX_LX 1024
+int  rbtp_plane_sums_noalloc(const double *ux, const double *uy, const double *uz, const double *phi,
+                             const int *owner, const double *particle_state, int npart, int lx,
+                             int ly, int lz, double t_hot, double t_cold, double *plane_sums,
+                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -157,6 +157,9 @@ SIGNATURES = [
     ("rbtp_write_flow", C.c_int, [_H, C.c_char_p, C.c_int]),
     ("rbtp_write_fg", C.c_int, [_H, C.c_char_p, C.c_int]),
     ("rbtp_write_particles", C.c_int, [_H, C.c_char_p, C.c_int]),
+    ("rbtp_plane_sums_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                          C.c_double, C.c_void_p, C.c_void_p]),
 ]
 
 _lib: Optional[C.CDLL] = None
