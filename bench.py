@@ -183,6 +183,36 @@ def e2e_variant(torch, name, storage, steps, dist=None):
             "seconds": sec, "includes": "state upload from host + K steps + Nu/means read-back"}
 
 
+def nu_accuracy(steps: int = 20000, every: int = 50) -> dict:
+    """Time-averaged Nusselt numbers of FP32 and shifted-FP16 storage against the FP64 path (the
+    parity-tested path) on 64x64x32, Ra=1e6, Pr=0.71, averaged over the second half of the run."""
+    import numpy as np
+    from rbtp import Solver, workloads as W
+    out = {"workload": "64x64x32 Ra=1e6 Pr=0.71, seeded start", "steps": steps, "sample_every": every}
+    series = {}
+    for st, name in ((0, "f64"), (1, "f32"), (2, "f16s")):
+        cfg = W.config("plain_fp64", storage=st)
+        s = Solver(cfg)
+        s.load_state(*W.initial_state(cfg))
+        rows = []
+        t0 = time.perf_counter()
+        for _ in range(steps // every):
+            s.step(every, macros_last=True)
+            rows.append(s.nu(s.istep))
+        series[name] = np.array(rows)
+        out[name + "_seconds"] = round(time.perf_counter() - t0, 3)
+        s.close()
+    half = slice(len(series["f64"]) // 2, None)
+    for name in ("f64", "f32", "f16s"):
+        r = series[name][half]
+        out[name] = {"nu_bulk": float(r[:, 2].mean()), "nu_top": float(r[:, 3].mean()),
+                     "nu_bottom": float(r[:, 4].mean())}
+    for name in ("f32", "f16s"):
+        out[name]["rel_err_vs_f64"] = {k: abs(out[name][k] / out["f64"][k] - 1.0)
+                                       for k in ("nu_bulk", "nu_top", "nu_bottom")}
+    return out
+
+
 def cpu_baseline(steps: int = 3, nz: int = 40):
     """The oracle (FP64 OpenMP restatement of the reference step) on a slab of the production
     grid, all host threads."""
@@ -256,6 +286,7 @@ def run_ours(args) -> dict:
     p64 = guarded(time_variant, torch, "particle_laden", 0, psteps, args.warmup, dist, rho_particle_ratio=1.0)
     p32 = guarded(time_variant, torch, "particle_laden", 1, psteps, args.warmup, dist, rho_particle_ratio=1.0)
     e2e = guarded(e2e_variant, torch, "production", 1, args.steps, dist)
+    nua = guarded(nu_accuracy) if rank == 0 else None
 
     def roof(v):
         b = bytes_per_node(["f64", "f32", "f16s"].index(v["storage"]))
@@ -283,6 +314,7 @@ def run_ours(args) -> dict:
         "e2e": e2e,
         "fp64": fp64, "fp16s": f16, "particle_laden_fp64": p64, "particle_laden_fp32": p32,
         "fp32_over_fp64": round(head["mlups"] / fp64["mlups"], 3) if "mlups" in fp64 else None,
+        "nu_accuracy": nua,
     }
     if rank == 0:
         try:

@@ -34,18 +34,23 @@ __device__ __forceinline__ double sq3(double dx, double dy, double dz)
     return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
 }
 
-// links.cu:7-23 with explicit rounding
+// links.cu:7-23 with explicit rounding.  The lattice direction has components in {-1, 0, 1}, so the
+// products c.d are exact and are formed by sign selection, |c|^2 is an exact small integer, and the
+// final division by 2|c|^2 is an exact scaling for |c|^2 = 1, 2; results are bit-identical to the
+// rounded double formula.
+__device__ __forceinline__ double csel(int c, double d) { return c == 0 ? 0.0 : (c > 0 ? d : -d); }
+
 __device__ __forceinline__ bool link_q(int cxi, int cyi, int czi, double x0, double y0, double z0,
                                        double px, double py, double pz, double rsq, double &q)
 {
-    const double cxd = (double)cxi, cyd = (double)cyi, czd = (double)czi;
     const double dx = dsub(x0, px), dy = dsub(y0, py), dz = dsub(z0, pz);
-    const double a = sq3(cxd, cyd, czd);
-    const double b = dmul(2.0, dadd(dadd(dmul(cxd, dx), dmul(cyd, dy)), dmul(czd, dz)));
+    const int a = cxi * cxi + cyi * cyi + czi * czi;
+    const double b = dmul(2.0, dadd(dadd(csel(cxi, dx), csel(cyi, dy)), csel(czi, dz)));
     const double c = dsub(sq3(dx, dy, dz), rsq);
-    const double disc = dsub(dmul(b, b), dmul(dmul(4.0, a), c));
+    const double disc = dsub(dmul(b, b), dmul((double)(4 * a), c));
     if (disc <= 0.0) return false;
-    q = __ddiv_rn(dsub(-b, __dsqrt_rn(disc)), dmul(2.0, a));
+    const double num = dsub(-b, __dsqrt_rn(disc));
+    q = (a == 3) ? __ddiv_rn(num, 6.0) : dmul(num, a == 1 ? 0.5 : 0.25);
     return (q >= 0.0 && q <= 1.0);
 }
 
@@ -151,7 +156,8 @@ __global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const 
         const double uwy = vy + (relx * wz - relz * wx);
         const double uwz = vz + (rely * wx - relx * wy);
         const double evel = cxi * uwx + cyi * uwy + czi * uwz;
-        const double mom = 2.0 * w * ph.rho0 * evel / RT;
+        const double mom = 2.0 * w * ph.rho0 * evel * (1.0 / RT);
+        const double inv_2q = (q >= 0.5) ? 0.5 / q : 0.0;
 
         const int ix1 = ix - cxi, iy1 = iy - cyi, iz1 = iz - czi;
         const bool in1 = ix1 >= 0 && ix1 < geo.lx && iy1 >= 0 && iy1 < geo.ly && iz1 >= 0 && iz1 < geo.lz;
@@ -168,7 +174,6 @@ __global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const 
                 fval = 2.0 * q * f_here + (1.0 - 2.0 * q) * f_up - mom;
             } else {
                 const double f_oc = (double)ST::ld_f(fB + (long long)o * L + x, w, ph.t0);
-                const double inv_2q = 0.5 / q;
                 fval = (f_here - mom) * inv_2q + (2.0 * q - 1.0) * inv_2q * f_oc;
             }
         } else {
@@ -181,7 +186,6 @@ __global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const 
                 gval = -(2.0 * q * g_here + (1.0 - 2.0 * q) * gu) + amp;
             } else {
                 const double go = (double)ST::ld_g(gB + (long long)o * L + x, w, ph.t0);
-                const double inv_2q = 0.5 / q;
                 gval = -g_here * inv_2q + amp * inv_2q + (2.0 * q - 1.0) * inv_2q * go;
             }
         } else {
@@ -197,11 +201,8 @@ __global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const 
                               : (double)ST::ld_f(fB + (long long)o * L + solid, w, ph.t0);
         const double g_out = (MODE == RBTP_STORE_F64) ? gval
                               : (double)ST::ld_g(gB + (long long)o * L + solid, w, ph.t0);
-        // ibb.cu:160-187 (force, torque) and 202-204 (heat)
-        const double crx = (double)ix + 0.5 + q * (double)cxi;
-        const double cry = (double)iy + 0.5 + q * (double)cyi;
-        const double crz = (double)iz + 0.5 + q * (double)czi;
-        const double rx = crx - px, ry = cry - py, rz = crz - pz;
+        // ibb.cu:160-187 (force, torque about the same intersection point) and 202-204 (heat)
+        const double rx = relx, ry = rely, rz = relz;
         const double Fx = (cxi - uwx) * f_here - (-cxi - uwx) * f_out;
         const double Fy = (cyi - uwy) * f_here - (-cyi - uwy) * f_out;
         const double Fz = (czi - uwz) * f_here - (-czi - uwz) * f_out;
@@ -501,6 +502,7 @@ __global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const
     // conservative single-precision shell test: a link needs |x - X| <= r + sqrt(3)
     const float reach = (float)r + 2.0f;
     const float reach2 = reach * reach;
+    const float pxf = (float)px, pyf = (float)py, pzf = (float)pz;
     int base = 0;
     for (int c0 = 0; c0 < total; c0 += LINK_THREADS) {
         const int t = c0 + threadIdx.x;
@@ -510,8 +512,8 @@ __global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const
             const int rem = t - lz * nx * ny;
             const int ly = rem / nx;
             const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
-            const float ddx = (float)((double)ix + 0.5 - px), ddy = (float)((double)iy + 0.5 - py),
-                        ddz = (float)((double)iz + 0.5 - pz);
+            const float ddx = ((float)ix + 0.5f) - pxf, ddy = ((float)iy + 0.5f) - pyf,
+                        ddz = ((float)iz + 0.5f) - pzf;
             const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
             if (ddx * ddx + ddy * ddy + ddz * ddz <= reach2 && owner[idx] < 0) {
                 unroll<26>([&](auto K) {
