@@ -183,17 +183,20 @@ def e2e_variant(torch, name, storage, steps, dist=None):
             "seconds": sec, "includes": "state upload from host + K steps + Nu/means read-back"}
 
 
-def nu_accuracy(steps: int = 20000, every: int = 50) -> dict:
+def nu_accuracy(steps: int = 60000, every: int = 100) -> dict:
     """Time-averaged Nusselt numbers of FP32 and shifted-FP16 storage against the FP64 path (the
-    parity-tested path) on 64x64x32, Ra=1e6, Pr=0.71, averaged over the second half of the run."""
+    parity-tested path) on 64x64x32, Ra=1e6, Pr=0.71, averaged over the last two thirds of the
+    run.  Convection at this Ra is chaotic, so a second FP64 run from a different seeded
+    perturbation gives the statistical noise floor of a time average of this length."""
     import numpy as np
     from rbtp import Solver, workloads as W
-    out = {"workload": "64x64x32 Ra=1e6 Pr=0.71, seeded start", "steps": steps, "sample_every": every}
+    out = {"workload": "64x64x32 Ra=1e6 Pr=0.71, seeded start", "steps": steps, "sample_every": every,
+           "average_over": "last 2/3 of the run"}
     series = {}
-    for st, name in ((0, "f64"), (1, "f32"), (2, "f16s")):
+    for st, name, seed in ((0, "f64", 1), (0, "f64_seed2", 2), (1, "f32", 1), (2, "f16s", 1)):
         cfg = W.config("plain_fp64", storage=st)
         s = Solver(cfg)
-        s.load_state(*W.initial_state(cfg))
+        s.load_state(*W.initial_state(cfg, seed=seed))
         rows = []
         t0 = time.perf_counter()
         for _ in range(steps // every):
@@ -202,12 +205,12 @@ def nu_accuracy(steps: int = 20000, every: int = 50) -> dict:
         series[name] = np.array(rows)
         out[name + "_seconds"] = round(time.perf_counter() - t0, 3)
         s.close()
-    half = slice(len(series["f64"]) // 2, None)
-    for name in ("f64", "f32", "f16s"):
-        r = series[name][half]
+    keep = slice(len(series["f64"]) // 3, None)
+    for name in series:
+        r = series[name][keep]
         out[name] = {"nu_bulk": float(r[:, 2].mean()), "nu_top": float(r[:, 3].mean()),
                      "nu_bottom": float(r[:, 4].mean())}
-    for name in ("f32", "f16s"):
+    for name in ("f64_seed2", "f32", "f16s"):
         out[name]["rel_err_vs_f64"] = {k: abs(out[name][k] / out["f64"][k] - 1.0)
                                        for k in ("nu_bulk", "nu_top", "nu_bottom")}
     return out
