@@ -196,6 +196,36 @@ int  rbtp_write_flow(rbtp_handle *h, const char *dir, int istep);        /* outp
 int  rbtp_write_fg(rbtp_handle *h, const char *dir, int istep);          /* output_fg     */
 int  rbtp_write_particles(rbtp_handle *h, const char *dir, int istep);   /* output_particles */
 
+/* ---- batched execution (spec addition: many cavities, one persistent launch) ---------- */
+/* A batch advances many independent cavities (own sizes, Ra, Pr, particle counts; one storage
+ * mode) in lockstep: per step ONE persistent launch of the fused step over a packed tile table of all
+ * cavities, one launch per particle kernel for all spheres of all cavities, the whole step captured
+ * once in a CUDA graph and replayed.  Members are ordinary handles (initialised before rbtp_batch_add);
+ * between batch steps every single-cavity call (exports, Nu, writers) works on them as usual.  The
+ * tile shape and persistent grid are chosen by an autotuner that times the candidates on the first
+ * steps of a batch (all candidates compute identical results).  Flow-output (dissipation) steps
+ * are not produced in batch mode; macroscopic fields are materialised on each member's NDIAG,
+ * NNUOUT, NFLOWOUT, NEND cadence and on its sampling cadence. */
+typedef struct rbtp_batch rbtp_batch;
+typedef struct rbtp_batch_stats {
+    int members, tiles, total_particles, tile_shape;   /* tile_shape: 0 = 32x4, 1 = 64x2 */
+    int grid, graph;                                    /* persistent blocks; 1 if replaying a graph */
+    int tuned, reserved;
+    double last_step_ms;                                /* device time of the last step (events) */
+    double nodes;                                       /* lattice nodes over all members */
+} rbtp_batch_stats;
+int  rbtp_batch_create(int storage, rbtp_batch **out);
+int  rbtp_batch_destroy(rbtp_batch *b);
+int  rbtp_batch_add(rbtp_batch *b, rbtp_handle *h);
+int  rbtp_batch_remove(rbtp_batch *b, rbtp_handle *h);
+/* Materialise h's macroscopic fields every `every` steps (0 = only its cfg cadence): the sampling
+ * that a serving loop uses for Nu time series. */
+int  rbtp_batch_set_sampling(rbtp_batch *b, rbtp_handle *h, int every);
+int  rbtp_batch_step(rbtp_batch *b, int nsteps);
+int  rbtp_batch_stats_get(rbtp_batch *b, rbtp_batch_stats *out);
+/* Force a tile shape (0/1) and persistent grid (blocks), or re-enable the autotuner with shape -1. */
+int  rbtp_batch_set_launch(rbtp_batch *b, int shape, int grid);
+
 /* ---- allocation-free diagnostic sums ----------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory — code hosted in
  * a framework that owns the whole device memory pool, or a loop that cannot afford the implicit

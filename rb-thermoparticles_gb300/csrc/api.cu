@@ -18,52 +18,11 @@
 #include <sys/types.h>
 #include <vector>
 
-#include "rbtp_internal.cuh"
+#include "handle.cuh"
+
 
 using namespace rbtp;
-
-namespace {
-
-constexpr int PHASE_HOME = 0;      // current buffer holds post-streaming populations
-constexpr int PHASE_COLLIDED = 1;  // current buffer holds post-collision populations + fix-ups
-
 constexpr int NP_COLS = RBTP_PARTICLE_COLS;
-
-}  // namespace
-
-struct rbtp_handle {
-    rbtp_config cfg;
-    rbtp_derived der;
-    Geo geo;
-    Phys ph;
-    int mode = RBTP_STORE_F64;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    void *f[2] = {nullptr, nullptr}, *g[2] = {nullptr, nullptr};
-    int cur = 0;
-    int phase = PHASE_HOME;
-    double *faux = nullptr, *rho_wall = nullptr;
-    double *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr, *phi = nullptr;
-    double *ted = nullptr, *ked = nullptr;
-    double *fcol = nullptr, *gcol = nullptr;  // FP64 scratch (collided copy / export / import)
-    DevStatus *status = nullptr;
-    DevStatus *status_host = nullptr;
-    // particles
-    PartBuffers pb{};
-    int *owner[2] = {nullptr, nullptr};
-    int ocur = 0;
-    // diagnostics
-    double *partials = nullptr, *plane = nullptr;
-    int nchunks = 1;
-    std::vector<double> plane_host;
-    bool plane_valid = false;
-    // bookkeeping
-    int istep = 0;
-    bool initialised = false;
-    bool macros_valid = false;
-    bool dissip_valid = false;
-    std::string err;
-};
 
 namespace {
 
@@ -167,6 +126,8 @@ int plane_sums(rbtp_handle *h)
 }
 
 }  // namespace
+
+void rbtp_batch_detach(rbtp_handle *h);  // batch.cu
 
 // =================================================================================================
 extern "C" {
@@ -293,7 +254,7 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
     CKC(cudaMemsetAsync(h->status, 0, sizeof(DevStatus), h->stream));
     CKC(cudaMallocHost(reinterpret_cast<void **>(&h->status_host), sizeof(DevStatus)));
     const long long rows = (long long)cfg->ly * cfg->lz;
-    h->nchunks = (int)std::min<long long>(rows, 1024);
+    h->nchunks = (int)std::min<long long>(rows, 512);
     CKC(dalloc(&h->partials, (size_t)h->nchunks * NPLANEQ * cfg->lx));
     CKC(dalloc(&h->plane, (size_t)NPLANEQ * cfg->lx));
 
@@ -318,7 +279,9 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
         CKC(dalloc(&pb.link_cnt, (size_t)np));
         CKC(cudaMemsetAsync(pb.link_cnt, 0, (size_t)np * sizeof(int), h->stream));
         const long long nf_bound = (long long)np * shell_bound(r, r + 1.7606816861659007);
-        pb.nf_cap = (int)std::min<long long>(nf_bound, std::max<long long>(65536, (long long)np * 512));
+        // a sphere uncovers a few nodes per step; 128 per sphere per step (or the shell bound) is
+        // far beyond any stable LBM velocity, and an overflow is reported, not written past
+        pb.nf_cap = (int)std::min<long long>(nf_bound, std::max<long long>(8192, (long long)np * 128));
         CKC(dalloc(&pb.nf_node, (size_t)pb.nf_cap)); CKC(dalloc(&pb.nf_pid, (size_t)pb.nf_cap));
         CKC(dalloc(&pb.nf_val, (size_t)pb.nf_cap * 54)); CKC(dalloc(&pb.nf_mac, (size_t)pb.nf_cap * 5));
         // contact cell list: cells no narrower than the interaction range 2r + REP_MIN_GAP
@@ -344,6 +307,7 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
 int rbtp_destroy(rbtp_handle *h)
 {
     if (!h) return RBTP_OK;
+    rbtp_batch_detach(h);
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (int k = 0; k < 2; ++k) { cudaFree(h->f[k]); cudaFree(h->g[k]); cudaFree(h->owner[k]); }
     cudaFree(h->faux); cudaFree(h->rho_wall);

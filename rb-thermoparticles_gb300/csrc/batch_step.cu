@@ -1,0 +1,121 @@
+// batch_step.cu — device side of batched execution: many independent cavities (any sizes, Ra, Pr,
+// particle counts, one storage mode) advanced by ONE persistent launch of the fused step over a
+// packed tile table, plus the small plan/advance kernels that keep each cavity's step state on the
+// device so that the whole step can be captured once in a CUDA graph and replayed.
+//
+// Tile table: int4 (cavity, tile_x, tile_y, z) for every TX x TY tile of every cavity, packed
+// cavity after cavity.  The persistent grid (chosen by the host autotuner, a multiple of the SM
+// count) walks the table with a grid stride, so small and large cavities share the machine without
+// per-cavity launches.
+#include "step_node.cuh"
+
+namespace rbtp {
+
+namespace {
+
+__device__ __forceinline__ bool hits(int istep, int every) { return every > 0 && istep % every == 0; }
+
+// Decide every cavity's output mode for the coming step (the cadence logic of main.cu:98-114 plus
+// the batch's sampling cadence) and reset the per-step particle counters.
+__global__ void k_batch_plan(CavDesc *desc, int n)
+{
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        CavDesc &d = desc[m];
+        const int istep = d.istep + 1;
+        const bool macro = hits(istep, d.ndiag) || hits(istep, d.nnuout) || hits(istep, d.nflowout) ||
+                           istep == d.nend || hits(istep, d.every);
+        d.out = macro ? OUT_MACROS : (d.pb.np > 0 ? OUT_RHO : OUT_NONE);
+        if (d.pb.np > 0) {
+            d.status->nf_count = 0;
+            d.status->ncontacts = 0;
+        }
+    }
+}
+
+__global__ void k_batch_advance(CavDesc *desc, int n)
+{
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+        CavDesc &d = desc[m];
+        d.cur ^= 1;
+        if (d.pb.np > 0) d.ocur ^= 1;
+        d.phase = 1;
+        d.istep += 1;
+    }
+}
+
+template <int MODE, bool PULL>
+__device__ __forceinline__ void step_out(const CavDesc &d, const StepBuffers &b, int out, int ix, int iy,
+                                         int iz)
+{
+    if (out == OUT_NONE) step_node<MODE, PULL, OUT_NONE>(d.geo, d.ph, b, ix, iy, iz);
+    else if (out == OUT_RHO) step_node<MODE, PULL, OUT_RHO>(d.geo, d.ph, b, ix, iy, iz);
+    else step_node<MODE, PULL, OUT_MACROS>(d.geo, d.ph, b, ix, iy, iz);
+}
+
+// The batched kernel carries all phase/output variants of the step body behind block-uniform
+// branches; it is given more registers than the single-cavity kernel (4 resident blocks of 128)
+// to keep them in registers.
+#ifndef RBTP_BATCH_MINB_LOW
+#define RBTP_BATCH_MINB_LOW 4
+#endif
+
+template <int MODE, int TX, int TY>
+__global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MINB_F64 : RBTP_BATCH_MINB_LOW)
+    k_step_batched(const CavDesc *__restrict__ desc, const int4 *__restrict__ tiles, int ntiles)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int4 tl = tiles[t];
+        const CavDesc &d = desc[tl.x];
+        const int ix = tl.y * TX + threadIdx.x, iy = tl.z * TY + threadIdx.y, iz = tl.w;
+        if (ix >= d.geo.lx || iy >= d.geo.ly) continue;
+        const int cur = d.cur;
+        StepBuffers b;
+        b.fin = d.f[cur];
+        b.gin = d.g[cur];
+        b.fout = d.f[cur ^ 1];
+        b.gout = d.g[cur ^ 1];
+        b.faux = d.faux;
+        b.rho_wall = d.rho_wall;
+        b.rho = d.rho; b.ux = d.ux; b.uy = d.uy; b.uz = d.uz; b.phi = d.phi;
+        b.fcol = nullptr; b.gcol = nullptr;
+        b.status = d.status;
+        if (d.phase) step_out<MODE, true>(d, b, d.out, ix, iy, iz);
+        else step_out<MODE, false>(d, b, d.out, ix, iy, iz);
+    }
+}
+
+template <int MODE>
+cudaError_t launch_mode(int shape, const CavDesc *desc, const int4 *tiles, int ntiles, int grid, cudaStream_t st)
+{
+    if (ntiles <= 0) return cudaSuccess;
+    if (shape == 0) k_step_batched<MODE, 32, 4><<<grid, dim3(32, 4, 1), 0, st>>>(desc, tiles, ntiles);
+    else k_step_batched<MODE, 64, 2><<<grid, dim3(64, 2, 1), 0, st>>>(desc, tiles, ntiles);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_batch_plan(CavDesc *desc, int n, cudaStream_t st)
+{
+    k_batch_plan<<<(n + 127) / 128, 128, 0, st>>>(desc, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_advance(CavDesc *desc, int n, cudaStream_t st)
+{
+    k_batch_advance<<<(n + 127) / 128, 128, 0, st>>>(desc, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step_batched(int mode, int shape, const CavDesc *desc, const int4 *tiles, int ntiles,
+                                int grid, cudaStream_t st)
+{
+    switch (mode) {
+    case RBTP_STORE_F64: return launch_mode<RBTP_STORE_F64>(shape, desc, tiles, ntiles, grid, st);
+    case RBTP_STORE_F32: return launch_mode<RBTP_STORE_F32>(shape, desc, tiles, ntiles, grid, st);
+    case RBTP_STORE_F16S: return launch_mode<RBTP_STORE_F16S>(shape, desc, tiles, ntiles, grid, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace rbtp

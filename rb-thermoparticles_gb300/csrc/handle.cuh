@@ -1,0 +1,53 @@
+// handle.cuh — the host-side state of one cavity (rbtp_handle), shared by the single-cavity C ABI
+// (api.cu) and batched execution (batch.cu).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "rbtp_internal.cuh"
+
+namespace rbtp {
+constexpr int PHASE_HOME = 0;      // current buffer holds post-streaming populations
+constexpr int PHASE_COLLIDED = 1;  // current buffer holds post-collision populations + fix-ups
+}  // namespace rbtp
+
+using namespace rbtp;
+
+struct rbtp_handle {
+    // batch membership (batch.cu)
+    struct rbtp_batch *batch = nullptr;
+    int sample_every = 0;
+    rbtp_config cfg;
+    rbtp_derived der;
+    Geo geo;
+    Phys ph;
+    int mode = RBTP_STORE_F64;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    void *f[2] = {nullptr, nullptr}, *g[2] = {nullptr, nullptr};
+    int cur = 0;
+    int phase = PHASE_HOME;
+    double *faux = nullptr, *rho_wall = nullptr;
+    double *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr, *phi = nullptr;
+    double *ted = nullptr, *ked = nullptr;
+    double *fcol = nullptr, *gcol = nullptr;  // FP64 scratch (collided copy / export / import)
+    DevStatus *status = nullptr;
+    DevStatus *status_host = nullptr;
+    // particles
+    PartBuffers pb{};
+    int *owner[2] = {nullptr, nullptr};
+    int ocur = 0;
+    // diagnostics
+    double *partials = nullptr, *plane = nullptr;
+    int nchunks = 1;
+    std::vector<double> plane_host;
+    bool plane_valid = false;
+    // bookkeeping
+    int istep = 0;
+    bool initialised = false;
+    bool macros_valid = false;
+    bool dissip_valid = false;
+    std::string err;
+};
+

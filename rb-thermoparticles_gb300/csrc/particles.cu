@@ -114,14 +114,12 @@ __device__ __forceinline__ void block_reduce_fixed(double (&v)[NQ], double *sh /
 constexpr int IBB_THREADS = 128;
 
 template <int MODE>
-__global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const Phys ph,
-                                                           const PartBuffers pb, void *f_,
-                                                           void *g_, const double *rho)
+__device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                                               const int *owner_cur, void *f_, void *g_,
+                                               const double *rho, int p, double *sh)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
-    __shared__ double sh[7 * IBB_THREADS];
-    const int p = blockIdx.x;
     const int np = pb.np;
     S *fB = static_cast<S *>(f_);
     S *gB = static_cast<S *>(g_);
@@ -162,7 +160,7 @@ __global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const 
         const int ix1 = ix - cxi, iy1 = iy - cyi, iz1 = iz - czi;
         const bool in1 = ix1 >= 0 && ix1 < geo.lx && iy1 >= 0 && iy1 < geo.ly && iz1 >= 0 && iz1 < geo.lz;
         const long long x1 = in1 ? ((long long)iz1 * geo.lxy + (long long)iy1 * geo.lx + ix1) : 0;
-        const bool fluid1 = in1 && pb.owner_cur[x1] < 0;
+        const bool fluid1 = in1 && owner_cur[x1] < 0;
 
         const double f_here = (double)ST::ld_f(fB + (long long)ip * L + x, w, ph.t0);
         const double g_here = (double)ST::ld_g(gB + (long long)ip * L + x, w, ph.t0);
@@ -222,6 +220,15 @@ __global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const 
     }
 }
 
+template <int MODE>
+__global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const Phys ph,
+                                                           const PartBuffers pb, void *f_,
+                                                           void *g_, const double *rho)
+{
+    __shared__ double sh[7 * IBB_THREADS];
+    links_ibb_body<MODE>(geo, ph, pb, pb.owner_cur, f_, g_, rho, blockIdx.x, sh);
+}
+
 // ------------------------------------------------------------------------------------------------
 // Contacts: cell list, ascending-partner sums (pforces.cu:6-76).
 // ------------------------------------------------------------------------------------------------
@@ -233,10 +240,8 @@ __device__ __forceinline__ int cell_of(double v, double cs, int n)
     return c;
 }
 
-__global__ void k_cell_count(const PartBuffers pb)
+__device__ __forceinline__ void cell_count_body(const PartBuffers &pb, int p)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= pb.np) return;
     const double *st = pb.state;
     const int cx = cell_of(PCOL(st, pb.np, 0, p), pb.cell_size, pb.ncell[0]);
     const int cy = cell_of(PCOL(st, pb.np, 1, p), pb.cell_size, pb.ncell[1]);
@@ -244,11 +249,15 @@ __global__ void k_cell_count(const PartBuffers pb)
     atomicAdd(&pb.cell_count[(cz * pb.ncell[1] + cy) * pb.ncell[0] + cx], 1);
 }
 
-__global__ void k_cell_scan(const PartBuffers pb, int ncells)
+__global__ void k_cell_count(const PartBuffers pb)
 {
-    // single block; sequential chunks with a block scan
-    __shared__ int sh[1024];
-    __shared__ int carry;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < pb.np) cell_count_body(pb, p);
+}
+
+// one block of up to 1024 threads; sequential chunks with a block scan
+__device__ __forceinline__ void cell_scan_body(const PartBuffers &pb, int ncells, int *sh, int &carry)
+{
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     for (int b = 0; b < ncells; b += blockDim.x) {
@@ -269,10 +278,15 @@ __global__ void k_cell_scan(const PartBuffers pb, int ncells)
     }
 }
 
-__global__ void k_cell_fill(const PartBuffers pb)
+__global__ void k_cell_scan(const PartBuffers pb, int ncells)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= pb.np) return;
+    __shared__ int sh[1024];
+    __shared__ int carry;
+    cell_scan_body(pb, ncells, sh, carry);
+}
+
+__device__ __forceinline__ void cell_fill_body(const PartBuffers &pb, int p)
+{
     const double *st = pb.state;
     const int cx = cell_of(PCOL(st, pb.np, 0, p), pb.cell_size, pb.ncell[0]);
     const int cy = cell_of(PCOL(st, pb.np, 1, p), pb.cell_size, pb.ncell[1]);
@@ -282,14 +296,18 @@ __global__ void k_cell_fill(const PartBuffers pb)
     pb.cell_items[pb.cell_start[c] + slot] = p;
 }
 
-constexpr int MAX_CAND = 64;
-
-__global__ void k_contact_force(const Geo geo, const Phys ph, const PartBuffers pb,
-                                DevStatus *status)
+__global__ void k_cell_fill(const PartBuffers pb)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < pb.np) cell_fill_body(pb, p);
+}
+
+constexpr int MAX_CAND = 64;
+
+__device__ __forceinline__ void contact_force_body(const Geo &geo, const Phys &ph,
+                                                   const PartBuffers &pb, DevStatus *status, int p)
+{
     const int np = pb.np;
-    if (p >= np) return;
     const double *st = pb.state;
     const double x = PCOL(st, np, 0, p), y = PCOL(st, np, 1, p), z = PCOL(st, np, 2, p);
     const double radius = ph.radius, coeff = ph.rep_coeff, min_gap = ph.min_gap;
@@ -371,14 +389,19 @@ __global__ void k_contact_force(const Geo geo, const Phys ph, const PartBuffers 
     pb.cF[2 * np + p] = dadd(fz, wfz);
 }
 
+__global__ void k_contact_force(const Geo geo, const Phys ph, const PartBuffers pb,
+                                DevStatus *status)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < pb.np) contact_force_body(geo, ph, pb, status, p);
+}
+
 // ------------------------------------------------------------------------------------------------
 // History shift + Newton-Euler + temperature (pforces.cu:80-116, ibb.cu:258-262, move.cu:5-103).
 // ------------------------------------------------------------------------------------------------
-__global__ void k_update(const Phys ph, const PartBuffers pb)
+__device__ __forceinline__ void update_body(const Phys &ph, const PartBuffers &pb, int p)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int np = pb.np;
-    if (p >= np) return;
     double *st = pb.state;
     const double dt = 1.0;
     const double buoyancy = (1.0 - 1.0 / ph.rho_ratio) * ph.grav0;
@@ -418,12 +441,18 @@ __global__ void k_update(const Phys ph, const PartBuffers pb)
     PCOL(st, np, 30, p) = PCOL(st, np, 30, p) + 0.5 * dt * (heat + heat_prev) / ph.heat_cap;
 }
 
+__global__ void k_update(const Phys ph, const PartBuffers pb)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < pb.np) update_body(ph, pb, p);
+}
+
 // ------------------------------------------------------------------------------------------------
 // Solid marking over all particles (links.cu:25-48, 160-188).
 // ------------------------------------------------------------------------------------------------
-__global__ void k_mark(const Geo geo, const Phys ph, const PartBuffers pb, int *owner)
+__device__ __forceinline__ void mark_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                                          int *owner, int p)
 {
-    const int p = blockIdx.x;
     const double *st = pb.state;
     const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
     const double r = ph.radius;
@@ -444,6 +473,11 @@ __global__ void k_mark(const Geo geo, const Phys ph, const PartBuffers pb, int *
         const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
         atomicMin(reinterpret_cast<unsigned int *>(owner) + idx, (unsigned int)p);
     }
+}
+
+__global__ void k_mark(const Geo geo, const Phys ph, const PartBuffers pb, int *owner)
+{
+    mark_body(geo, ph, pb, owner, blockIdx.x);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -480,13 +514,10 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total
     return wbase + incl - v;
 }
 
-__global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const Phys ph,
-                                                            const PartBuffers pb, const int *owner,
-                                                            DevStatus *status)
+__device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                                               const int *owner, DevStatus *status, int p, int *wsum,
+                                               int *cand /* (box-local node index << 5) | direction */)
 {
-    __shared__ int wsum[LINK_THREADS / 32];
-    __shared__ int cand[LINK_CAND];  // (box-local node index << 5) | direction
-    const int p = blockIdx.x;
     const double *st = pb.state;
     const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
     const double r = ph.radius;
@@ -570,13 +601,22 @@ __global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const
     if (threadIdx.x == 0) pb.link_cnt[p] = base;
 }
 
+__global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const Phys ph,
+                                                            const PartBuffers pb, const int *owner,
+                                                            DevStatus *status)
+{
+    __shared__ int wsum[LINK_THREADS / 32];
+    __shared__ int cand[LINK_CAND];
+    link_fill_body(geo, ph, pb, owner, status, blockIdx.x, wsum, cand);
+}
+
 // ------------------------------------------------------------------------------------------------
 // New-fluid detection (refill.cu:8-76), per particle around its new position.
 // ------------------------------------------------------------------------------------------------
-__global__ void k_new_fluid(const Geo geo, const Phys ph, const PartBuffers pb,
-                            const int *owner_prev, const int *owner_cur, DevStatus *status)
+__device__ __forceinline__ void new_fluid_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                                               const int *owner_prev, const int *owner_cur,
+                                               DevStatus *status, int p)
 {
-    const int p = blockIdx.x;
     const double *st = pb.state;
     const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
     const double r = ph.radius;
@@ -602,25 +642,30 @@ __global__ void k_new_fluid(const Geo geo, const Phys ph, const PartBuffers pb,
     }
 }
 
+__global__ void k_new_fluid(const Geo geo, const Phys ph, const PartBuffers pb,
+                            const int *owner_prev, const int *owner_cur, DevStatus *status)
+{
+    new_fluid_body(geo, ph, pb, owner_prev, owner_cur, status, blockIdx.x);
+}
+
 // Refill values (refill.cu:78-240): one warp per new-fluid node, lane ip computes population ip
 // from the post-collision populations of previous-step fluid neighbours (home slots of the
 // buffer just written by the step kernel).
 template <int MODE>
-__global__ void k_refill_compute(const Geo geo, const Phys ph, const PartBuffers pb,
-                                 const int *owner_prev, const void *f_, const void *g_,
-                                 const DevStatus *status)
+__device__ __forceinline__ void refill_compute_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                                                    const int *owner_prev, const void *f_, const void *g_,
+                                                    const DevStatus *status, int warp0, int nwarps)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
     const S *fB = static_cast<const S *>(f_);
     const S *gB = static_cast<const S *>(g_);
     const int lane = threadIdx.x & 31;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const int count = min(status->nf_count, pb.nf_cap);
     const long long L = geo.L;
     const double RT = 1.0 / 3.0;
     const double lambda0 = 1.0 - dweight(0);
-    for (int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; n < count; n += nwarps) {
+    for (int n = warp0; n < count; n += nwarps) {
         const int idx = pb.nf_node[n];
         const int iz = idx / (int)geo.lxy;
         const int iy = (idx - iz * (int)geo.lxy) / geo.lx;
@@ -717,12 +762,22 @@ __global__ void k_refill_compute(const Geo geo, const Phys ph, const PartBuffers
     }
 }
 
+template <int MODE>
+__global__ void k_refill_compute(const Geo geo, const Phys ph, const PartBuffers pb,
+                                 const int *owner_prev, const void *f_, const void *g_,
+                                 const DevStatus *status)
+{
+    refill_compute_body<MODE>(geo, ph, pb, owner_prev, f_, g_, status,
+                              (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
+}
+
 // Scatter the refill values into the slots the next pull reads at each new-fluid node.
 template <int MODE>
-__global__ void k_refill_scatter(const Geo geo, const Phys ph, const PartBuffers pb, void *f_,
-                                 void *g_, double *faux, const double *rho_wall, bool macros,
-                                 double *rho, double *ux, double *uy, double *uz, double *phi,
-                                 const DevStatus *status)
+__device__ __forceinline__ void refill_scatter_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+                                                    void *f_, void *g_, double *faux,
+                                                    const double *rho_wall, bool macros, double *rho,
+                                                    double *ux, double *uy, double *uz, double *phi,
+                                                    const DevStatus *status, long long t0, long long stride)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
@@ -732,8 +787,7 @@ __global__ void k_refill_scatter(const Geo geo, const Phys ph, const PartBuffers
     const int count = min(status->nf_count, pb.nf_cap);
     const long long L = geo.L;
     const long long total = (long long)count * 27;
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
+    for (long long t = t0; t < total; t += stride) {
         const int n = (int)(t / 27);
         const int ip = (int)(t - (long long)n * 27);
         const int idx = pb.nf_node[n];
@@ -770,6 +824,17 @@ __global__ void k_refill_scatter(const Geo geo, const Phys ph, const PartBuffers
             }
         }
     }
+}
+
+template <int MODE>
+__global__ void k_refill_scatter(const Geo geo, const Phys ph, const PartBuffers pb, void *f_,
+                                 void *g_, double *faux, const double *rho_wall, bool macros,
+                                 double *rho, double *ux, double *uy, double *uz, double *phi,
+                                 const DevStatus *status)
+{
+    refill_scatter_body<MODE>(geo, ph, pb, f_, g_, faux, rho_wall, macros, rho, ux, uy, uz, phi, status,
+                              (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                              (long long)gridDim.x * blockDim.x);
 }
 
 }  // namespace
@@ -851,6 +916,163 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
     RBTP_MODE_DISPATCH(mode, (k_refill_compute<M><<<152, 256, 0, st>>>(geo, ph, pb, owner_prev, f, g, status)));
     RBTP_MODE_DISPATCH(mode, (k_refill_scatter<M><<<152, 256, 0, st>>>(geo, ph, pb, f, g, faux, rho_wall, macros, rho, ux, uy, uz, phi, status)));
     return cudaGetLastError();
+}
+
+// =================================================================================================
+// Batched particle pipeline: the same per-particle bodies, with (cavity, particle) taken from a
+// packed particle map and each cavity's buffers and step state from its device descriptor.  The
+// populations of the current step are in buffer cur ^ 1 (the step kernel wrote them), the solid
+// flags of the previous build in owner[ocur] and the new ones go to owner[ocur ^ 1].
+// =================================================================================================
+namespace {
+
+template <int MODE>
+__global__ void __launch_bounds__(IBB_THREADS) k_links_ibb_b(const CavDesc *desc, const int2 *pmap)
+{
+    __shared__ double sh[7 * IBB_THREADS];
+    const int2 mp = pmap[blockIdx.x];
+    const CavDesc &d = desc[mp.x];
+    const int w = d.cur ^ 1;
+    links_ibb_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f[w], d.g[w], d.rho, mp.y, sh);
+}
+
+__global__ void k_cells_zero_b(const CavDesc *desc, const int *pmem)
+{
+    const CavDesc &d = desc[pmem[blockIdx.y]];
+    const int n = d.pb.ncell[0] * d.pb.ncell[1] * d.pb.ncell[2];
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+        d.pb.cell_count[c] = 0;
+        d.pb.cell_fill[c] = 0;
+    }
+}
+
+__global__ void k_cell_count_b(const CavDesc *desc, const int2 *pmap, int total)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    const int2 mp = pmap[g];
+    cell_count_body(desc[mp.x].pb, mp.y);
+}
+
+__global__ void k_cell_scan_b(const CavDesc *desc, const int *pmem)
+{
+    __shared__ int sh[1024];
+    __shared__ int carry;
+    const CavDesc &d = desc[pmem[blockIdx.x]];
+    cell_scan_body(d.pb, d.pb.ncell[0] * d.pb.ncell[1] * d.pb.ncell[2], sh, carry);
+}
+
+__global__ void k_cell_fill_b(const CavDesc *desc, const int2 *pmap, int total)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    const int2 mp = pmap[g];
+    cell_fill_body(desc[mp.x].pb, mp.y);
+}
+
+__global__ void k_contact_force_b(const CavDesc *desc, const int2 *pmap, int total)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    const int2 mp = pmap[g];
+    const CavDesc &d = desc[mp.x];
+    contact_force_body(d.geo, d.ph, d.pb, d.status, mp.y);
+}
+
+__global__ void k_update_b(const CavDesc *desc, const int2 *pmap, int total)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    const int2 mp = pmap[g];
+    const CavDesc &d = desc[mp.x];
+    update_body(d.ph, d.pb, mp.y);
+}
+
+__global__ void k_owner_fill_b(const CavDesc *desc, const int *pmem)
+{
+    const CavDesc &d = desc[pmem[blockIdx.y]];
+    int *o = d.owner[d.ocur ^ 1];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.geo.L;
+         i += (long long)gridDim.x * blockDim.x)
+        o[i] = -1;
+}
+
+__global__ void k_mark_b(const CavDesc *desc, const int2 *pmap)
+{
+    const int2 mp = pmap[blockIdx.x];
+    const CavDesc &d = desc[mp.x];
+    mark_body(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], mp.y);
+}
+
+__global__ void __launch_bounds__(LINK_THREADS) k_link_fill_b(const CavDesc *desc, const int2 *pmap)
+{
+    __shared__ int wsum[LINK_THREADS / 32];
+    __shared__ int cand[LINK_CAND];
+    const int2 mp = pmap[blockIdx.x];
+    const CavDesc &d = desc[mp.x];
+    link_fill_body(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], d.status, mp.y, wsum, cand);
+}
+
+__global__ void k_new_fluid_b(const CavDesc *desc, const int2 *pmap)
+{
+    const int2 mp = pmap[blockIdx.x];
+    const CavDesc &d = desc[mp.x];
+    new_fluid_body(d.geo, d.ph, d.pb, d.owner[d.ocur], d.owner[d.ocur ^ 1], d.status, mp.y);
+}
+
+template <int MODE>
+__global__ void k_refill_compute_b(const CavDesc *desc, const int *pmem)
+{
+    const CavDesc &d = desc[pmem[blockIdx.y]];
+    const int w = d.cur ^ 1;
+    refill_compute_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f[w], d.g[w], d.status,
+                              (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
+}
+
+template <int MODE>
+__global__ void k_refill_scatter_b(const CavDesc *desc, const int *pmem)
+{
+    const CavDesc &d = desc[pmem[blockIdx.y]];
+    const int w = d.cur ^ 1;
+    refill_scatter_body<MODE>(d.geo, d.ph, d.pb, d.f[w], d.g[w], d.faux, d.rho_wall, d.out == OUT_MACROS,
+                              d.rho, d.ux, d.uy, d.uz, d.phi, d.status,
+                              (long long)blockIdx.x * blockDim.x + threadIdx.x,
+                              (long long)gridDim.x * blockDim.x);
+}
+
+template <int MODE>
+cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int total, const int *pmem,
+                                   int npmem, cudaStream_t st)
+{
+    const int t = 128, bl = (total + t - 1) / t;
+    k_links_ibb_b<MODE><<<total, IBB_THREADS, 0, st>>>(desc, pmap);
+    k_cells_zero_b<<<dim3(4, npmem), 256, 0, st>>>(desc, pmem);
+    k_cell_count_b<<<bl, t, 0, st>>>(desc, pmap, total);
+    k_cell_scan_b<<<npmem, 1024, 0, st>>>(desc, pmem);
+    k_cell_fill_b<<<bl, t, 0, st>>>(desc, pmap, total);
+    k_contact_force_b<<<bl, t, 0, st>>>(desc, pmap, total);
+    k_update_b<<<bl, t, 0, st>>>(desc, pmap, total);
+    k_owner_fill_b<<<dim3(64, npmem), 256, 0, st>>>(desc, pmem);
+    k_mark_b<<<total, 256, 0, st>>>(desc, pmap);
+    k_link_fill_b<<<total, LINK_THREADS, 0, st>>>(desc, pmap);
+    k_new_fluid_b<<<total, 256, 0, st>>>(desc, pmap);
+    k_refill_compute_b<MODE><<<dim3(8, npmem), 256, 0, st>>>(desc, pmem);
+    k_refill_scatter_b<MODE><<<dim3(8, npmem), 256, 0, st>>>(desc, pmem);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_particles_batched(int mode, const CavDesc *desc, const int2 *pmap, int total_np,
+                                     const int *pmem, int npmem, cudaStream_t st)
+{
+    if (total_np <= 0 || npmem <= 0) return cudaSuccess;
+    switch (mode) {
+    case RBTP_STORE_F64: return particles_batched_mode<RBTP_STORE_F64>(desc, pmap, total_np, pmem, npmem, st);
+    case RBTP_STORE_F32: return particles_batched_mode<RBTP_STORE_F32>(desc, pmap, total_np, pmem, npmem, st);
+    case RBTP_STORE_F16S: return particles_batched_mode<RBTP_STORE_F16S>(desc, pmap, total_np, pmem, npmem, st);
+    }
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace rbtp

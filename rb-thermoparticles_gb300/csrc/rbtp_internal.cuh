@@ -275,6 +275,34 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
 cudaError_t launch_initial_owner(const Geo &geo, const Phys &ph, const PartBuffers &pb,
                                  int *owner, cudaStream_t st);
 
+// ------------------------------------------------------------------------------------------------
+// Batched execution: one descriptor per cavity in device memory.  The step state (buffer parity,
+// owner parity, phase, step counter, this step's output mode) lives on the device and is advanced by
+// the batch kernels themselves, so a captured CUDA graph can be replayed step after step.
+// ------------------------------------------------------------------------------------------------
+struct CavDesc {
+    Geo geo;
+    Phys ph;
+    void *f[2], *g[2];
+    double *faux, *rho_wall, *rho, *ux, *uy, *uz, *phi;
+    DevStatus *status;
+    PartBuffers pb;
+    int *owner[2];
+    int cur, ocur, phase, istep;        // advanced on the device
+    int ndiag, nnuout, nflowout, nend;  // output cadence (<= 0: never)
+    int every;                          // extra macro cadence (sampling), <= 0: never
+    int out;                            // this step's output mode (written by the plan kernel)
+    int mode, pad;
+};
+
+constexpr int BATCH_SHAPES = 2;  // tile shapes of the batched step: 0 = 32x4, 1 = 64x2
+cudaError_t launch_batch_plan(CavDesc *desc, int n, cudaStream_t st);
+cudaError_t launch_batch_advance(CavDesc *desc, int n, cudaStream_t st);
+cudaError_t launch_step_batched(int mode, int shape, const CavDesc *desc, const int4 *tiles,
+                                int ntiles, int grid, cudaStream_t st);
+cudaError_t launch_particles_batched(int mode, const CavDesc *desc, const int2 *pmap, int total_np,
+                                     const int *pmem, int npmem, cudaStream_t st);
+
 // Diagnostics ------------------------------------------------------------------------------------
 // Per-x-plane sums: 10 quantities x lx, see diagnostics.cu.
 constexpr int NPLANEQ = 10;

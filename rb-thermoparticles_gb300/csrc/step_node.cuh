@@ -1,0 +1,192 @@
+// step_node.cuh — the per-node body of the fused pull-stream/collide step (see lbm_step.cu for the
+// algorithm and its reference mapping).  Included by lbm_step.cu (single cavity) and batch_step.cu
+// (many cavities over a packed tile table), which instantiate it for their launch shapes.
+#pragma once
+
+#include "rbtp_internal.cuh"
+
+// Resident 128-thread blocks per SM requested from the register allocator (FP64 is bound by the
+// FP64 pipe, the FP32/FP16 storage modes by HBM bandwidth).
+#ifndef RBTP_STEP_MINB_F64
+#define RBTP_STEP_MINB_F64 1
+#endif
+#ifndef RBTP_STEP_MINB_LOW
+#define RBTP_STEP_MINB_LOW 6  // 6 x 128 threads (<= 80 registers): best of a 1/5/6/8 sweep on GB300
+#endif
+
+namespace rbtp {
+
+// One node of the fused step; shared by the single-cavity kernel below and the batched kernel of
+// batch.cu.  (ix, iy, iz) must lie inside the lattice.
+template <int MODE, bool PULL, int OUT>
+__device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const StepBuffers &b, int ix,
+                                          int iy, int iz)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    using R = typename ST::R;
+    const long long L = geo.L;
+    const long long node = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
+    const S *__restrict__ fin = static_cast<const S *>(b.fin);
+    const S *__restrict__ gin = static_cast<const S *>(b.gin);
+    S *__restrict__ fout = static_cast<S *>(b.fout);
+    S *__restrict__ gout = static_cast<S *>(b.gout);
+    const double t0 = ph.t0;
+    const bool xlo = ix == 0, xhi = ix == geo.lx - 1;
+    const bool ylo = iy == 0, yhi = iy == geo.ly - 1;
+    const bool zlo = iz == 0, zhi = iz == geo.lz - 1;
+    const long long wall_slot = (long long)iz * geo.ly + iy;
+    const StepK<R> &K = step_consts<R>(ph);
+
+    R f[27], g[27];
+    unroll<27>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i), o = dopp(i);
+        constexpr double w = dweight(i);
+        if constexpr (!PULL || i == 0) {
+            f[i] = ST::ld_f(fin + (long long)i * L + node, w, t0);
+            g[i] = ST::ld_g(gin + (long long)i * L + node, w, t0);
+        } else {
+            // f_i(x) = f*_i(x - c_i); a neighbour outside the box returns f*_opp(x) (bounce-back)
+            const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
+                             (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
+            const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
+            const long long src = out ? ((long long)o * L + node) : ((long long)i * L + node - off);
+            f[i] = ST::ld_f(fin + src, w, t0);
+            g[i] = ST::ld_g(gin + src, w, t0);
+        }
+    });
+    if constexpr (PULL) {
+        // streaming.cu:45-61: at the x walls a direction that leaves only through x takes the
+        // Dirichlet anti-bounce-back with the node's density deviation of the previous step; y/z
+        // exits stay adiabatic.  Only warps holding x-wall nodes enter this branch.
+        if (xlo || xhi) {
+            const R rw = (R)b.rho_wall[(xhi ? (long long)geo.lz * geo.ly : 0) + wall_slot];
+            const R tw = xlo ? K.thot : K.tcold;
+            unroll<27>([&](auto I) {
+                constexpr int i = decltype(I)::value;
+                constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+                if constexpr (cx != 0) {
+                    const bool ox = (cx == 1) ? xlo : xhi;
+                    const bool oyz = (cy == 1 && ylo) || (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
+                    if (ox && !oyz) g[i] = wall_image(g[i], dweight(i), tw, rw);
+                }
+            });
+        }
+    }
+
+    // ---- moments (macrovar.cu:3-34), pairwise ----
+    R rho = f[0], jx = 0, jy = 0, jz = 0;
+    R phi = g[0], kx = 0, ky = 0, kz = 0;
+    unroll<13>([&](auto Kp) {
+        constexpr int i = dpair(decltype(Kp)::value);
+        constexpr int o = dopp(i);
+        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+        const R sf = f[i] + f[o], df = f[i] - f[o];
+        const R sg = g[i] + g[o], dg = g[i] - g[o];
+        rho += sf;
+        phi += sg;
+        if constexpr (cx == 1) { jx += df; kx += dg; }
+        if constexpr (cx == -1) { jx -= df; kx -= dg; }
+        if constexpr (cy == 1) { jy += df; ky += dg; }
+        if constexpr (cy == -1) { jy -= df; ky -= dg; }
+        if constexpr (cz == 1) { jz += df; kz += dg; }
+        if constexpr (cz == -1) { jz -= df; kz -= dg; }
+    });
+    if (!(fabs(rho) < (R)1e30) || !(fabs(phi) < (R)1e30)) atomicOr(&b.status->nonfinite, 1);
+
+    const R fold = (R)b.faux[node];
+    const R ux = jx + (R)0.5 * fold, uy = jy, uz = jz;
+    // forcing (macrovar.cu:45): F_x = g0 beta (phi - T0); F_y = F_z = 0 always
+    const R Fx = K.g0b * (phi - K.t0);
+    b.faux[node] = (double)Fx;
+
+    if constexpr (OUT >= OUT_MACROS) {
+        b.rho[node] = (double)rho;
+        b.ux[node] = (double)ux;
+        b.uy[node] = (double)uy;
+        b.uz[node] = (double)uz;
+        b.phi[node] = (double)phi;
+    } else if constexpr (OUT == OUT_RHO) {
+        b.rho[node] = (double)rho;
+    }
+    if (xlo) b.rho_wall[wall_slot] = (double)rho;
+    if (xhi) b.rho_wall[(long long)geo.lz * geo.ly + wall_slot] = (double)rho;
+
+    // ---- f collision (collision.cu:3-33) ----
+    // f*_i = om f_i + w_i [ (rho + P_i)/tau + G (c_ix - u_x)(1 + P_i) ],  P_i = A_i + B_i,
+    // A = 4.5 (c.u)^2 - 1.5 u^2, B = 3 c.u, G = 3 (1 - 1/(2 tau)) F_x.
+    const R G = K.Gc * Fx;
+    const R Gux = G * ux;
+    const R h = (R)1.5 * (ux * ux + uy * uy + uz * uz);
+    const R k1 = K.tinv - Gux;
+    const R k0 = rho * K.tinv - Gux;
+    // ---- g collision (collision.cu:35-89) ----
+    // g*_i = omc g_i + geqnew_i / tauc + w_i c_i.V, with the source vector
+    // V = Rc [ -2 rho/gd (sum_i c_i g_i - phi u) + x F_x phi (3 - rho/gd) ],  gd = rho/3 + 2 tauc/3.
+    const R gd = rho * (R)(1.0 / 3.0) + K.gd0;
+    const R rgd = rho / gd;
+    const R c2 = (R)(-2) * rgd * K.Rc;
+    const R Vx = c2 * (kx - phi * ux) + K.Rc * Fx * phi * ((R)3 - rgd);
+    const R Vy = c2 * (ky - phi * uy);
+    const R Vz = c2 * (kz - phi * uz);
+    const R pt = phi * K.tcinv;
+    const R ptb = pt * ((R)1 + rho);
+
+    {
+        constexpr R w0 = (R)dweight(0);
+        f[0] = K.om * f[0] + w0 * (k0 - h * k1);
+        g[0] = K.omc * g[0] + (w0 * (ptb - pt * h) - pt * rho);
+    }
+    // Pairs grouped by weight class (face, edge, corner); the class constants fold w_i into the
+    // per-node coefficients and live only while their class is processed.
+    unroll<3>([&](auto C) {
+        constexpr int c = decltype(C)::value + 1;
+        constexpr R w = (R)(c == 1 ? 2.0 / 27.0 : (c == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
+        const R wk1 = w * k1;
+        const R ca = (R)4.5 * wk1, cb = w * k0 - h * wk1, c3 = (R)3 * wk1;
+        const R wG = w * G;
+        const R ce = (R)4.5 * wG, cd = wG - h * wG, cg = (R)3 * wG;
+        const R wpt = w * pt;
+        const R ga = (R)4.5 * wpt, gb = w * ptb - h * wpt, gc = (R)3 * wpt;
+        const R vx = w * Vx, vy = w * Vy, vz = w * Vz;
+        unroll<13>([&](auto Kp) {
+            constexpr int i = dpair(decltype(Kp)::value);
+            if constexpr (dclass(i) == c) {
+                constexpr int o = dopp(i);
+                constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+                R cu = 0, cV = 0;
+                if constexpr (cx != 0) { cu += (R)cx * ux; cV += (R)cx * vx; }
+                if constexpr (cy != 0) { cu += (R)cy * uy; cV += (R)cy * vy; }
+                if constexpr (cz != 0) { cu += (R)cz * uz; cV += (R)cz * vz; }
+                const R q = cu * cu;
+                R wS = q * ca + cb;                 // w (A k1 + k0)
+                R wD = cu * c3;                     // w B k1
+                if constexpr (cx != 0) {
+                    wS += (R)cx * (cu * cg);        // w cx G B
+                    wD += (R)cx * (q * ce + cd);    // w cx G (1 + A)
+                }
+                const R gS = q * ga + gb;           // w pt (1 + rho + A)
+                const R gD = cu * gc + cV;          // w pt B + w c.V
+                const R fi = f[i], fo = f[o], gi = g[i], go = g[o];
+                f[i] = K.om * fi + (wS + wD);
+                f[o] = K.om * fo + (wS - wD);
+                g[i] = K.omc * gi + (gS + gD);
+                g[o] = K.omc * go + (gS - gD);
+            }
+        });
+    });
+
+    unroll<27>([&](auto I) {
+        constexpr int i = decltype(I)::value;
+        constexpr double w = dweight(i);
+        ST::st_f(fout + (long long)i * L + node, f[i], w, t0);
+        ST::st_g(gout + (long long)i * L + node, g[i], w, t0);
+        if constexpr (OUT == OUT_MACROS_COL) {
+            b.fcol[(long long)i * L + node] = (double)f[i];
+            b.gcol[(long long)i * L + node] = (double)g[i];
+        }
+    });
+}
+
+}  // namespace rbtp

@@ -117,6 +117,12 @@ class NuRow(C.Structure):
         return tuple(getattr(self, n) for n, _ in self._fields_)
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("members", C.c_int), ("tiles", C.c_int), ("total_particles", C.c_int),
+                ("tile_shape", C.c_int), ("grid", C.c_int), ("graph", C.c_int), ("tuned", C.c_int),
+                ("reserved", C.c_int), ("last_step_ms", C.c_double), ("nodes", C.c_double)]
+
+
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int)
 _H = C.c_void_p
@@ -157,6 +163,14 @@ SIGNATURES = [
     ("rbtp_write_flow", C.c_int, [_H, C.c_char_p, C.c_int]),
     ("rbtp_write_fg", C.c_int, [_H, C.c_char_p, C.c_int]),
     ("rbtp_write_particles", C.c_int, [_H, C.c_char_p, C.c_int]),
+    ("rbtp_batch_create", C.c_int, [C.c_int, C.POINTER(_H)]),
+    ("rbtp_batch_destroy", C.c_int, [_H]),
+    ("rbtp_batch_add", C.c_int, [_H, _H]),
+    ("rbtp_batch_remove", C.c_int, [_H, _H]),
+    ("rbtp_batch_set_sampling", C.c_int, [_H, _H, C.c_int]),
+    ("rbtp_batch_step", C.c_int, [_H, C.c_int]),
+    ("rbtp_batch_stats_get", C.c_int, [_H, C.POINTER(BatchStats)]),
+    ("rbtp_batch_set_launch", C.c_int, [_H, C.c_int, C.c_int]),
     ("rbtp_plane_sums_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                           C.c_double, C.c_void_p, C.c_void_p]),
@@ -369,10 +383,57 @@ class Solver:
         _check(self.lib.rbtp_write_particles(self._h, _b(directory), istep), self._h)
 
 
+class Batch:
+    """Many cavities advanced in lockstep by one persistent launch per step (rbtp_batch_*)."""
+
+    def __init__(self, storage: int = STORE_F32):
+        self.lib = load_library()
+        self._b = C.c_void_p()
+        _check(self.lib.rbtp_batch_create(storage, C.byref(self._b)))
+        self.members = []
+
+    def add(self, solver: "Solver", sample_every: int = 0) -> None:
+        st = self.lib.rbtp_batch_add(self._b, solver.handle)
+        if st:
+            raise RbtpError(st, "rbtp_batch_add")
+        self.members.append(solver)
+        if sample_every:
+            _check(self.lib.rbtp_batch_set_sampling(self._b, solver.handle, sample_every))
+
+    def remove(self, solver: "Solver") -> None:
+        _check(self.lib.rbtp_batch_remove(self._b, solver.handle))
+        self.members.remove(solver)
+
+    def step(self, nsteps: int = 1) -> None:
+        st = self.lib.rbtp_batch_step(self._b, nsteps)
+        if st:
+            raise RbtpError(st, "rbtp_batch_step")
+
+    def set_launch(self, shape: int, grid: int = 0) -> None:
+        _check(self.lib.rbtp_batch_set_launch(self._b, shape, grid))
+
+    def stats(self) -> dict:
+        st = BatchStats()
+        _check(self.lib.rbtp_batch_stats_get(self._b, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_ if f != "reserved"}
+
+    def close(self) -> None:
+        if self._b:
+            self.lib.rbtp_batch_destroy(self._b)
+            self._b = C.c_void_p()
+            self.members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _b(s: Optional[str]):
     return s.encode() if s else None
 
 
-__all__ = ["Config", "Derived", "NuRow", "Solver", "RbtpError", "load_library", "derive",
+__all__ = ["Config", "Derived", "NuRow", "Solver", "Batch", "BatchStats", "RbtpError", "load_library", "derive",
            "STORE_F64", "STORE_F32", "STORE_F16S", "PARTICLE_COLS", "PARTICLE_COLUMNS",
            "SIGNATURES", "LIB_PATH"]

@@ -83,3 +83,29 @@ def initial_state(cfg: Config, seed: int = 1, amp: float = 1e-3):
     flow7 = np.zeros(7 * L)
     flow7[4 * L:5 * L] = T
     return f, g, flow7
+
+
+def ensemble(n: int = 256, seed: int = 2, storage: int = 1, max_spheres: int = 200,
+             sizes=(32, 48, 64, 96, 128)):
+    """Configurations of the batched ensemble: LY drawn from `sizes`, LX = LY, LZ = LY/2, Ra
+    log-uniform in [1e5, 1e8], Pr uniform in [0.7, 7], VISC by the u0 rule, 0..max_spheres spheres of
+    diameter 0.1 LY (density ratio 1.0, the reference default), per-cavity placement seeds."""
+    rng = np.random.default_rng(seed)
+    cfgs = []
+    for k in range(n):
+        ly = int(rng.choice(sizes))
+        lx, lz = ly, ly // 2
+        ra = float(10.0 ** rng.uniform(5.0, 8.0))
+        pr = float(rng.uniform(0.7, 7.0))
+        ns = int(rng.integers(0, max_spheres + 1))
+        r = 0.5 * 0.1 * lx
+        vol = 4.0 * math.pi * r ** 3 / 3.0
+        # the densest rejection-sampled packing is bounded; keep the fraction workable
+        ns = min(ns, int(0.15 * lx * ly * lz / vol))
+        over = dict(lx=lx, ly=ly, lz=lz, rayleigh=ra, prandtl=pr)
+        if ns > 0:
+            over.update(activate_particles=1, particle_diam_frac=0.1,
+                        particle_fraction=(ns + 0.5) * vol / (lx * ly * lz), rho_particle_ratio=1.0,
+                        particle_rand_seed=86143 + k)
+        cfgs.append(config("plain_fp64", storage=storage, **over))
+    return cfgs

@@ -25,7 +25,7 @@ LIBDIR = os.path.join(HERE, "rbtp", "_lib")
 LIB = os.path.join(LIBDIR, "librbtp.so")
 RB3D = os.path.join(LIBDIR, "rb3d")
 
-SOURCES = ["lbm_step.cu", "particles.cu", "diagnostics.cu", "api.cu", "noalloc.cu"]
+SOURCES = ["lbm_step.cu", "batch_step.cu", "particles.cu", "diagnostics.cu", "api.cu", "batch.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
@@ -78,7 +78,8 @@ def build(jobs: int = 0, host: bool = True, verbose: bool = False) -> str:
     _arch_guard()
     os.makedirs(LIBDIR, exist_ok=True)
     nv = nvcc()
-    headers = [os.path.join(CSRC, "rbtp_internal.cuh"), os.path.join(REPO, "include", "rbtp.h")]
+    headers = [os.path.join(CSRC, h) for h in ("rbtp_internal.cuh", "step_node.cuh", "handle.cuh")]
+    headers.append(os.path.join(REPO, "include", "rbtp.h"))
     objs, todo = [], []
     for src in SOURCES:
         s = os.path.join(CSRC, src)

@@ -1,0 +1,97 @@
+"""Batched execution (rbtp_batch_*): cavities of different sizes, Ra, Pr and sphere counts advanced
+together by one persistent launch per step must give the same results as each cavity stepped
+alone.  Tolerances: FP64 storage 1e-12 relative L2 of the populations (the batched kernel runs the
+same per-node code, so agreement is normally exact); FP32 storage 1e-6.  Particle integer
+structures (solid owners) must be identical.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from rbtp import Batch, Solver, STORE_F32, STORE_F64, workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfgs(storage):
+    return [
+        W.config("plain_fp64", lx=40, ly=32, lz=16, rayleigh=3e5, storage=storage),
+        W.config("plain_fp64", lx=24, ly=48, lz=20, rayleigh=2e6, prandtl=3.0, storage=storage),
+        W.config("plain_fp64", lx=48, ly=48, lz=24, activate_particles=1, particle_diam_frac=8.0 / 48.0,
+                 particle_fraction=0.04, storage=storage),
+        W.config("plain_fp64", lx=32, ly=32, lz=32, activate_particles=1, particle_diam_frac=6.0 / 32.0,
+                 particle_fraction=0.03, rayleigh=5e5, particle_rand_seed=7, storage=storage),
+    ]
+
+
+def _start(cfg, k):
+    s = Solver(cfg)
+    if cfg.activate_particles:
+        s.initialize()
+        f, g, f7 = W.initial_state(cfg, seed=20 + k)
+        s.load_state(f, g, f7, s.particles())
+    else:
+        s.load_state(*W.initial_state(cfg, seed=20 + k))
+    return s
+
+
+@pytest.mark.parametrize("storage,tol", [(STORE_F64, 1e-12), (STORE_F32, 1e-6)])
+def test_batch_matches_individual_runs(lib_built, storage, tol):
+    cfgs = _cfgs(storage)
+    alone = [_start(c, k) for k, c in enumerate(cfgs)]
+    mixed = [_start(c, k) for k, c in enumerate(cfgs)]
+    b = Batch(storage)
+    for s in mixed:
+        b.add(s)
+    for s in alone:
+        s.step(25)
+    b.step(25)
+    st = b.stats()
+    assert st["members"] == 4 and st["tuned"] == 1 and st["graph"] == 1
+    for a, m in zip(alone, mixed):
+        assert m.istep == a.istep == 25
+        fa, ga = a.fg()
+        fm, gm = m.fg()
+        assert rel_l2(gm, ga) < tol
+        assert np.linalg.norm(fm - fa) / np.linalg.norm(ga) < tol
+        if a.npart:
+            assert np.array_equal(a.flags(), m.flags())
+            pa, pm = a.particles(), m.particles()
+            assert np.abs(pa - pm).max() <= 1e3 * tol * max(1.0, np.abs(pa).max())
+
+
+def test_launch_shapes_give_identical_results(lib_built):
+    cfgs = _cfgs(STORE_F32)
+    outs = []
+    for shape, grid in ((0, 152 * 4), (1, 152 * 8), (0, 100000)):
+        ss = [_start(c, k) for k, c in enumerate(cfgs)]
+        b = Batch(STORE_F32)
+        for s in ss:
+            b.add(s)
+        b.set_launch(shape, grid)
+        b.step(12)
+        outs.append([s.fg()[1] for s in ss])
+        b.close()
+    for o in outs[1:]:
+        for x, y in zip(outs[0], o):
+            assert np.array_equal(x, y)
+
+
+def test_membership_changes_and_sampling(lib_built):
+    cfgs = _cfgs(STORE_F32)
+    ss = [_start(c, k) for k, c in enumerate(cfgs)]
+    ref = [_start(c, k) for k, c in enumerate(cfgs)]
+    b = Batch(STORE_F32)
+    b.add(ss[0], sample_every=10)
+    b.add(ss[2], sample_every=10)
+    b.step(10)
+    assert ss[0].nu(10)[0] == 10.0        # macros materialised by the sampling cadence
+    b.add(ss[1], sample_every=5)           # joins while the others are running
+    b.remove(ss[0])                        # leaves; keeps its state and stays usable alone
+    b.step(10)
+    ss[0].step(10)
+    for k, steps in ((0, 20), (1, 10), (2, 20)):
+        ref[k].step(steps)
+        assert ss[k].istep == ref[k].istep
+        assert rel_l2(ss[k].fg()[1], ref[k].fg()[1]) < 1e-6
+    assert ss[1].nu(ss[1].istep)[0] == 10.0
