@@ -220,6 +220,52 @@ def batch_variant(torch, steps: int, warmup: int, n: int = 256) -> dict:
     return out
 
 
+def serving_variant(n: int = 16, rate: float = 4.0, seed: int = 3, tick: int = 250,
+                    batched_mlups=None) -> dict:
+    """Serving: n solve requests drawn like the batched ensemble (sizes, Ra, Pr, spheres) with
+    horizons uniform in [2000, 50000] steps and Nu sampled every 500 steps, arriving as a Poisson
+    stream of the given rate (requests/s), admitted by footprint within 180 GB, FP32 storage.
+    Latency = completion - scheduled arrival (server clock)."""
+    import numpy as np
+    from rbtp import Server, workloads as W
+    rng = np.random.default_rng(seed)
+    cfgs = W.ensemble(n, seed=seed, storage=1)
+    horizons = rng.integers(2000, 50001, size=n)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    srv = Server(1, hbm_budget=180e9)
+    t0 = srv.stats()["clock"]
+    ids, k, peak = [], 0, 0
+    while True:
+        now = srv.stats()["clock"] - t0
+        while k < n and arrivals[k] <= now:
+            ids.append(srv.submit(cfgs[k], int(horizons[k]), 500))
+            k += 1
+        a, q = srv.tick(tick)
+        peak = max(peak, a)
+        if k == n and a == 0 and q == 0:
+            break
+        if a == 0 and q == 0 and k < n:
+            time.sleep(max(0.0, min(0.05, arrivals[k] - (srv.stats()["clock"] - t0))))
+    st = srv.stats()
+    lat, ok = [], 0
+    for i, rid in enumerate(ids):
+        p = srv.poll(rid)
+        _, _, done = srv.times(rid)
+        if p["state"] == Server.DONE:
+            ok += 1
+            lat.append(done - t0 - arrivals[i])
+    span = st["clock"] - t0 - arrivals[0]
+    served = st["node_updates"] / span / 1e6
+    out = {"requests": n, "completed": ok, "rate_per_s": rate, "tick_steps": tick,
+           "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+           "served_mlups": served, "peak_active": peak, "makespan_s": round(span, 3),
+           "node_updates": st["node_updates"]}
+    if batched_mlups:
+        out["served_over_batched"] = served / batched_mlups
+    srv.close()
+    return out
+
+
 def nu_accuracy(steps: int = 60000, every: int = 100) -> dict:
     """Time-averaged Nusselt numbers of FP32 and shifted-FP16 storage against the FP64 path (the
     parity-tested path) on 64x64x32, Ra=1e6, Pr=0.71, averaged over the last two thirds of the
@@ -328,6 +374,7 @@ def run_ours(args) -> dict:
     e2e = guarded(e2e_variant, torch, "production", 1, args.steps, dist)
     nua = guarded(nu_accuracy) if rank == 0 else None
     bat = guarded(batch_variant, torch, args.steps, args.warmup)
+    srv = guarded(serving_variant, batched_mlups=bat.get("mlups"))
 
     def roof(v):
         b = bytes_per_node(["f64", "f32", "f16s"].index(v["storage"]))
@@ -357,6 +404,7 @@ def run_ours(args) -> dict:
         "fp32_over_fp64": round(head["mlups"] / fp64["mlups"], 3) if "mlups" in fp64 else None,
         "nu_accuracy": nua,
         "batched_ensemble": bat,
+        "serving": srv,
     }
     if rank == 0:
         try:

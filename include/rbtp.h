@@ -226,6 +226,34 @@ int  rbtp_batch_stats_get(rbtp_batch *b, rbtp_batch_stats *out);
 /* Force a tile shape (0/1) and persistent grid (blocks), or re-enable the autotuner with shape -1. */
 int  rbtp_batch_set_launch(rbtp_batch *b, int shape, int grid);
 
+/* Device bytes rbtp_create allocates for cfg (the admission currency of the server below). */
+int  rbtp_footprint(const rbtp_config *cfg, size_t *bytes);
+
+/* ---- continuous-batching solve server (spec addition) ------------------------------------ */
+/* Requests (case, horizon in steps, Nu sampling cadence) are queued from any thread; each tick
+ * admits queued requests in arrival order while their footprint fits the HBM budget (and the
+ * active-slot limit, 0 = none), advances all active requests together in one batch by as many steps
+ * as none of them needs to stop for (at most max_steps), appends a Nu row (rbtp_nu_row, step =
+ * the request's own step) at each request's sample steps and at its last step, and retires finished
+ * requests.  State stays resident between ticks; results do not depend on the other requests. */
+typedef struct rbtp_server rbtp_server;
+#define RBTP_REQ_QUEUED 0
+#define RBTP_REQ_ACTIVE 1
+#define RBTP_REQ_DONE   2
+#define RBTP_REQ_FAILED 3
+int  rbtp_server_create(int storage, double hbm_budget_bytes, int max_active, rbtp_server **out);
+int  rbtp_server_destroy(rbtp_server *s);
+int  rbtp_server_submit(rbtp_server *s, const rbtp_config *cfg, int horizon, int sample_every, int *id);
+int  rbtp_server_tick(rbtp_server *s, int max_steps, int *nactive, int *nqueued);
+/* Copies up to cap Nu rows produced so far (the series streams while the request runs); returns the
+ * request's status (RBTP_OK unless it failed). */
+int  rbtp_server_poll(rbtp_server *s, int id, int *state, int *steps_done, rbtp_nu_row *rows, int cap,
+                      int *nrows);
+/* Server-clock seconds of submission, admission and completion (-1 if not reached yet). */
+int  rbtp_server_request_times(rbtp_server *s, int id, double *t_submit, double *t_admit, double *t_done);
+int  rbtp_server_stats(rbtp_server *s, double *node_updates, double *steps, double *used_bytes,
+                       double *clock);
+
 /* ---- allocation-free diagnostic sums ----------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory — code hosted in
  * a framework that owns the whole device memory pool, or a loop that cannot afford the implicit

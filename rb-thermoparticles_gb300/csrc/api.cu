@@ -191,6 +191,40 @@ int rbtp_derive(const rbtp_config *c, rbtp_derived *d)
 
 const char *rbtp_last_error(const rbtp_handle *h) { return h ? h->err.c_str() : "null handle"; }
 
+// Device bytes rbtp_create allocates for a config (the same sizes as below; the FP64 export scratch
+// that rbtp_get_fg / flow-output steps add on demand is not included).
+int rbtp_footprint(const rbtp_config *cfg, size_t *bytes)
+{
+    if (!cfg || !bytes) return RBTP_ERR_ARG;
+    rbtp_derived d;
+    rbtp_derive(cfg, &d);
+    const size_t L = (size_t)cfg->lx * cfg->ly * cfg->lz;
+    const size_t P = 27 * L;
+    const size_t sb = store_bytes(cfg->storage);
+    size_t b = 4 * P * sb;                                   // f, g double-buffered
+    b += 8 * L * sizeof(double);                             // faux, rho, ux, uy, uz, phi, ted, ked
+    b += 2 * (size_t)cfg->ly * cfg->lz * sizeof(double);     // rho_wall
+    const size_t rows = (size_t)cfg->ly * cfg->lz;
+    b += (std::min<size_t>(rows, 512) * NPLANEQ + NPLANEQ) * cfg->lx * sizeof(double);
+    const int np = cfg->activate_particles ? d.npart : 0;
+    if (np > 0) {
+        const double r = d.particle_radius;
+        b += (size_t)np * (NP_COLS + 10) * sizeof(double);   // state, hF, hT, hQ, cF
+        b += 2 * L * sizeof(int);                             // owner maps
+        const size_t lcap = (size_t)std::min<long long>(26 * shell_bound(r, r + std::sqrt(3.0)), 1LL << 30);
+        b += (size_t)np * lcap * (2 * sizeof(int) + sizeof(double)) + np * sizeof(int);
+        const long long nf_bound = (long long)np * shell_bound(r, r + 1.7606816861659007);
+        const size_t nfc = (size_t)std::min<long long>(nf_bound, std::max<long long>(8192, (long long)np * 128));
+        b += nfc * (2 * sizeof(int) + 59 * sizeof(double));
+        const double cs = 2.0 * r + std::max(cfg->rep_min_gap, 0.0) + 1e-9;
+        size_t nc = 1;
+        for (int a : {cfg->lx, cfg->ly, cfg->lz}) nc *= (size_t)std::max(1, (int)std::floor(a / cs));
+        b += 3 * nc * sizeof(int) + np * sizeof(int) + 2 * (size_t)np * 32 * sizeof(int);
+    }
+    *bytes = b;
+    return RBTP_OK;
+}
+
 int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
 {
     if (!cfg || !out) return RBTP_ERR_ARG;

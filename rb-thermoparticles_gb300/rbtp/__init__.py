@@ -171,6 +171,14 @@ SIGNATURES = [
     ("rbtp_batch_step", C.c_int, [_H, C.c_int]),
     ("rbtp_batch_stats_get", C.c_int, [_H, C.POINTER(BatchStats)]),
     ("rbtp_batch_set_launch", C.c_int, [_H, C.c_int, C.c_int]),
+    ("rbtp_footprint", C.c_int, [C.POINTER(Config), C.POINTER(C.c_size_t)]),
+    ("rbtp_server_create", C.c_int, [C.c_int, C.c_double, C.c_int, C.POINTER(_H)]),
+    ("rbtp_server_destroy", C.c_int, [_H]),
+    ("rbtp_server_submit", C.c_int, [_H, C.POINTER(Config), C.c_int, C.c_int, _IP]),
+    ("rbtp_server_tick", C.c_int, [_H, C.c_int, _IP, _IP]),
+    ("rbtp_server_poll", C.c_int, [_H, C.c_int, _IP, _IP, C.POINTER(NuRow), C.c_int, _IP]),
+    ("rbtp_server_request_times", C.c_int, [_H, C.c_int, _DP, _DP, _DP]),
+    ("rbtp_server_stats", C.c_int, [_H, _DP, _DP, _DP, _DP]),
     ("rbtp_plane_sums_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                           C.c_double, C.c_void_p, C.c_void_p]),
@@ -430,10 +438,66 @@ class Batch:
             pass
 
 
+def footprint(cfg: Config) -> int:
+    b = C.c_size_t()
+    _check(load_library().rbtp_footprint(C.byref(cfg), C.byref(b)))
+    return b.value
+
+
+class Server:
+    """Continuous-batching solve server (rbtp_server_*): submit cases, tick, stream Nu series."""
+
+    QUEUED, ACTIVE, DONE, FAILED = 0, 1, 2, 3
+
+    def __init__(self, storage: int = STORE_F32, hbm_budget: float = 180e9, max_active: int = 0):
+        self.lib = load_library()
+        self._s = C.c_void_p()
+        _check(self.lib.rbtp_server_create(storage, float(hbm_budget), max_active, C.byref(self._s)))
+
+    def submit(self, cfg: Config, horizon: int, sample_every: int) -> int:
+        rid = C.c_int()
+        _check(self.lib.rbtp_server_submit(self._s, C.byref(cfg), horizon, sample_every, C.byref(rid)))
+        return rid.value
+
+    def tick(self, max_steps: int = 100):
+        a, q = C.c_int(), C.c_int()
+        _check(self.lib.rbtp_server_tick(self._s, max_steps, C.byref(a), C.byref(q)))
+        return a.value, q.value
+
+    def poll(self, rid: int):
+        st, done, n = C.c_int(), C.c_int(), C.c_int()
+        self.lib.rbtp_server_poll(self._s, rid, C.byref(st), C.byref(done), None, 0, C.byref(n))
+        rows = (NuRow * max(n.value, 1))()
+        status = self.lib.rbtp_server_poll(self._s, rid, C.byref(st), C.byref(done), rows, n.value, C.byref(n))
+        series = np.array([r.as_tuple() for r in rows[:n.value]]).reshape(-1, 7)
+        return {"state": st.value, "steps_done": done.value, "status": status, "series": series}
+
+    def times(self, rid: int):
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        _check(self.lib.rbtp_server_request_times(self._s, rid, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def stats(self) -> dict:
+        v = [C.c_double() for _ in range(4)]
+        _check(self.lib.rbtp_server_stats(self._s, *[C.byref(x) for x in v]))
+        return dict(zip(["node_updates", "steps", "used_bytes", "clock"], [x.value for x in v]))
+
+    def close(self) -> None:
+        if self._s:
+            self.lib.rbtp_server_destroy(self._s)
+            self._s = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _b(s: Optional[str]):
     return s.encode() if s else None
 
 
-__all__ = ["Config", "Derived", "NuRow", "Solver", "Batch", "BatchStats", "RbtpError", "load_library", "derive",
+__all__ = ["Config", "Derived", "NuRow", "Solver", "Batch", "BatchStats", "Server", "footprint", "RbtpError", "load_library", "derive",
            "STORE_F64", "STORE_F32", "STORE_F16S", "PARTICLE_COLS", "PARTICLE_COLUMNS",
            "SIGNATURES", "LIB_PATH"]
