@@ -32,8 +32,8 @@ struct rbtp_batch {
     int *d_pmem = nullptr;
     int npmem = 0;
     bool dirty = true;
-    // launch configuration
-    int shape = 0, grid = 0;
+    // launch configuration (grid_factor: persistent blocks per SM, 0 = one block per tile)
+    int shape = 0, grid = 0, grid_factor = 8;
     bool tuned = false, forced = false;
     std::vector<std::pair<int, int>> cand;  // (shape, grid)
     std::vector<float> cand_ms;
@@ -126,14 +126,12 @@ int rebuild(rbtp_batch *b)
     b->cand.clear();
     b->cand_ms.clear();
     for (int s = 0; s < BATCH_SHAPES; ++s) {
-        for (int f : {4, 8, 16}) b->cand.push_back({s, std::min(b->ntiles[s], f * b->sms)});
-        b->cand.push_back({s, b->ntiles[s]});
+        for (int f : {4, 8, 16}) b->cand.push_back({s, f});
+        b->cand.push_back({s, 0});
     }
-    if (!b->forced) {
-        b->tuned = false;
-        b->shape = 0;
-        b->grid = std::min(b->ntiles[0], 8 * b->sms);
-    }
+    // a tuned choice survives membership changes (a serving loop changes them constantly)
+    if (!b->forced) b->grid = b->grid_factor > 0 ? std::min(b->ntiles[b->shape], b->grid_factor * b->sms)
+                                                 : b->ntiles[b->shape];
     b->dirty = false;
     return RBTP_OK;
 }
@@ -322,6 +320,7 @@ int rbtp_batch_set_launch(rbtp_batch *b, int shape, int grid)
     b->tuned = true;
     b->shape = shape;
     b->grid = grid;
+    b->grid_factor = -1;
     drop_graph(b);
     return RBTP_OK;
 }
@@ -337,12 +336,13 @@ int rbtp_batch_step(rbtp_batch *b, int nsteps)
     // autotuning: each candidate runs one warm step and one timed step
     while (!b->tuned && done < nsteps) {
         const size_t k = b->cand_ms.size();
-        const auto c = b->cand[k];
-        BCK(enqueue_step(b, c.first, c.second));
+        const int cs = b->cand[k].first, cf = b->cand[k].second;
+        const int cg = cf > 0 ? std::min(b->ntiles[cs], cf * b->sms) : b->ntiles[cs];
+        BCK(enqueue_step(b, cs, cg));
         ++done;
         if (done >= nsteps) break;
         BCK(cudaEventRecord(b->e0, b->stream));
-        BCK(enqueue_step(b, c.first, c.second));
+        BCK(enqueue_step(b, cs, cg));
         BCK(cudaEventRecord(b->e1, b->stream));
         BCK(cudaEventSynchronize(b->e1));
         float ms = 0.f;
@@ -352,7 +352,9 @@ int rbtp_batch_step(rbtp_batch *b, int nsteps)
         if (b->cand_ms.size() == b->cand.size()) {
             const size_t best = std::min_element(b->cand_ms.begin(), b->cand_ms.end()) - b->cand_ms.begin();
             b->shape = b->cand[best].first;
-            b->grid = b->cand[best].second;
+            b->grid_factor = b->cand[best].second;
+            b->grid = b->grid_factor > 0 ? std::min(b->ntiles[b->shape], b->grid_factor * b->sms)
+                                         : b->ntiles[b->shape];
             b->tuned = true;
             drop_graph(b);
         }
