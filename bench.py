@@ -36,6 +36,14 @@ MEASURED_PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_step launch on the
+# 320x320x160 single-phase workload, from a one-pass ncu capture of
+# `python bench.py --only production:<storage> --steps 3 --warmup 3`
+# (profiles/k_step_dram_320x320x160.md).  Algorithmic bytes per launch: 16,384,000 nodes x
+# bytes_per_node.
+NCU_DRAM_BYTES = {"f32": 3.69e9 + 3.70e9}
+
+
 def bytes_per_node(storage: int) -> int:
     """Algorithmic HBM bytes per lattice-node update: read+write 27 f and 27 g populations plus
     read+write of the FP64 buoyancy auxiliary F_x."""
@@ -379,9 +387,11 @@ def run_ours(args) -> dict:
     def roof(v):
         b = bytes_per_node(["f64", "f32", "f16s"].index(v["storage"]))
         achieved = v["nodes"] * b / (v["ms_per_step"] * 1e-3) / 1e9
+        traffic = NCU_DRAM_BYTES.get(v["storage"]) if v["workload"] == "production" else None
         return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_src,
-                "bytes_per_node": b, "traffic": None}
+                "bytes_per_node": b, "traffic": traffic,
+                "algorithmic_bytes": v["nodes"] * b}
 
     for v in (head, fp64, f16, p64, p32):
         if "error" not in v:

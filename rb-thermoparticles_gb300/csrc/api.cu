@@ -89,7 +89,7 @@ int read_status(rbtp_handle *h)
 int build_links(rbtp_handle *h, int *owner)
 {
     CK(launch_mark(h->geo, h->ph, h->pb, owner, h->stream));
-    CK(launch_link_fill(h->geo, h->ph, h->pb, owner, h->status, h->stream));
+    CK(launch_link_fill(h->mode, h->geo, h->ph, h->pb, owner, h->status, h->stream));
     return RBTP_OK;
 }
 

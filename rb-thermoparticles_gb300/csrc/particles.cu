@@ -54,6 +54,24 @@ __device__ __forceinline__ bool link_q(int cxi, int cyi, int czi, double x0, dou
     return (q >= 0.0 && q <= 1.0);
 }
 
+// Single-precision ray-sphere q for the FP32/FP16 storage modes (same formula, float arithmetic).
+// Returns 1 (link, q set) or -1 when the float result is too close to a decision edge (grazing
+// ray, q near 0 or 1); the caller then takes the exact FP64 test, so the set of links is the FP64
+// one in every storage mode and only the q values carry float rounding.
+__device__ __forceinline__ int link_q_f32(int cxi, int cyi, int czi, float dx, float dy, float dz,
+                                          float rsq, double &q)
+{
+    const int a = cxi * cxi + cyi * cyi + czi * czi;
+    const float b = 2.0f * ((cxi * dx + cyi * dy) + czi * dz);
+    const float c = (dx * dx + dy * dy + dz * dz) - rsq;
+    const float disc = b * b - (float)(4 * a) * c;
+    if (!(disc > 1.0e-3f * rsq)) return -1;
+    const float qf = (-b - sqrtf(disc)) * (1.0f / (float)(2 * a));
+    if (!(qf > 1.0e-3f && qf < 0.999f)) return -1;
+    q = (double)qf;
+    return 1;
+}
+
 // floor to int with the argument clamped first, so non-finite or far-away particle coordinates give
 // empty (clipped) boxes instead of overflowing integer arithmetic; NaN maps to -1e9.
 __device__ __forceinline__ int ifloor(double v)
@@ -132,12 +150,17 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
     const int n = min(pb.link_cnt[p], pb.link_cap);
     const long long base = (long long)p * pb.link_cap;
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    const double RT = 1.0 / 3.0;
+    // Per-link arithmetic in the storage mode's arithmetic type (double for FP64 storage, float
+    // otherwise); force, torque and heat accumulate in FP64 in every mode.
+    using RR = typename ST::R;
+    const RR vxr = (RR)vx, vyr = (RR)vy, vzr = (RR)vz, wxr = (RR)wx, wyr = (RR)wy, wzr = (RR)wz;
+    const float mom_k = (float)(2.0 * ph.rho0 * 3.0);   // 2 rho0 / c_s^2 (float modes)
+    const RR Tpr = (RR)Tp;
 
     for (int t = threadIdx.x; t < n; t += IBB_THREADS) {
         const int x = pb.link_node[base + t];
         const int ip = pb.link_dir[base + t];
-        const double q = pb.link_q[base + t];
+        const RR q = (RR)pb.link_q[base + t];
         const int iz = x / (int)geo.lxy;
         const int rem = x - iz * (int)geo.lxy;
         const int iy = rem / geo.lx;
@@ -145,46 +168,57 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
         const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
         const int o = dopp_rt(ip);
         const double w = dweight_rt(ip);
-        // moving wall velocity at the intersection point (ibb.cu:33-46)
-        const double cpx = (double)ix + 0.5 + q * cxi;
-        const double cpy = (double)iy + 0.5 + q * cyi;
-        const double cpz = (double)iz + 0.5 + q * czi;
-        const double relx = cpx - px, rely = cpy - py, relz = cpz - pz;
-        const double uwx = vx + (relz * wy - rely * wz);
-        const double uwy = vy + (relx * wz - relz * wx);
-        const double uwz = vz + (rely * wx - relx * wy);
-        const double evel = cxi * uwx + cyi * uwy + czi * uwz;
-        const double mom = 2.0 * w * ph.rho0 * evel * (1.0 / RT);
-        const double inv_2q = (q >= 0.5) ? 0.5 / q : 0.0;
+        const RR wr = (RR)w;
+        // moving wall velocity at the intersection point (ibb.cu:33-46); in the float modes the
+        // node-centre offset is formed in FP64 (absolute coordinates) and then rounded once
+        RR relx, rely, relz;
+        if constexpr (MODE == RBTP_STORE_F64) {
+            relx = ((double)ix + 0.5 + q * cxi) - px;
+            rely = ((double)iy + 0.5 + q * cyi) - py;
+            relz = ((double)iz + 0.5 + q * czi) - pz;
+        } else {
+            relx = (RR)((double)ix + 0.5 - px) + q * (RR)cxi;
+            rely = (RR)((double)iy + 0.5 - py) + q * (RR)cyi;
+            relz = (RR)((double)iz + 0.5 - pz) + q * (RR)czi;
+        }
+        const RR uwx = vxr + (relz * wyr - rely * wzr);
+        const RR uwy = vyr + (relx * wzr - relz * wxr);
+        const RR uwz = vzr + (rely * wxr - relx * wyr);
+        const RR evel = (RR)cxi * uwx + (RR)cyi * uwy + (RR)czi * uwz;
+        RR mom;
+        if constexpr (MODE == RBTP_STORE_F64) mom = 2.0 * w * ph.rho0 * evel * 3.0;
+        else mom = wr * mom_k * evel;
+        const RR inv_2q = (q >= (RR)0.5) ? (RR)0.5 / q : (RR)0;
 
         const int ix1 = ix - cxi, iy1 = iy - cyi, iz1 = iz - czi;
         const bool in1 = ix1 >= 0 && ix1 < geo.lx && iy1 >= 0 && iy1 < geo.ly && iz1 >= 0 && iz1 < geo.lz;
         const long long x1 = in1 ? ((long long)iz1 * geo.lxy + (long long)iy1 * geo.lx + ix1) : 0;
         const bool fluid1 = in1 && owner_cur[x1] < 0;
 
-        const double f_here = (double)ST::ld_f(fB + (long long)ip * L + x, w, ph.t0);
-        const double g_here = (double)ST::ld_g(gB + (long long)ip * L + x, w, ph.t0);
-        double fval, gval;
+        const RR f_here = ST::ld_f(fB + (long long)ip * L + x, w, ph.t0);
+        const RR g_here = ST::ld_g(gB + (long long)ip * L + x, w, ph.t0);
+        const RR one = (RR)1, two = (RR)2;
+        RR fval, gval;
         // ibb.cu:52-73 (f: q < 0.5), ibb.cu:114-128 (g: q <= 0.5)
         if (fluid1) {
-            if (q < 0.5) {
-                const double f_up = (double)ST::ld_f(fB + (long long)ip * L + x1, w, ph.t0);
-                fval = 2.0 * q * f_here + (1.0 - 2.0 * q) * f_up - mom;
+            if (q < (RR)0.5) {
+                const RR f_up = ST::ld_f(fB + (long long)ip * L + x1, w, ph.t0);
+                fval = two * q * f_here + (one - two * q) * f_up - mom;
             } else {
-                const double f_oc = (double)ST::ld_f(fB + (long long)o * L + x, w, ph.t0);
-                fval = (f_here - mom) * inv_2q + (2.0 * q - 1.0) * inv_2q * f_oc;
+                const RR f_oc = ST::ld_f(fB + (long long)o * L + x, w, ph.t0);
+                fval = (f_here - mom) * inv_2q + (two * q - one) * inv_2q * f_oc;
             }
         } else {
             fval = f_here - mom;
         }
-        const double amp = 2.0 * w * Tp * (1.0 + rho[x]);
+        const RR amp = two * wr * Tpr * (RR)(1.0 + rho[x]);
         if (fluid1) {
-            if (q <= 0.5) {
-                const double gu = (double)ST::ld_g(gB + (long long)ip * L + x1, w, ph.t0);
-                gval = -(2.0 * q * g_here + (1.0 - 2.0 * q) * gu) + amp;
+            if (q <= (RR)0.5) {
+                const RR gu = ST::ld_g(gB + (long long)ip * L + x1, w, ph.t0);
+                gval = -(two * q * g_here + (one - two * q) * gu) + amp;
             } else {
-                const double go = (double)ST::ld_g(gB + (long long)o * L + x, w, ph.t0);
-                gval = -g_here * inv_2q + amp * inv_2q + (2.0 * q - 1.0) * inv_2q * go;
+                const RR go = ST::ld_g(gB + (long long)o * L + x, w, ph.t0);
+                gval = -g_here * inv_2q + amp * inv_2q + (two * q - one) * inv_2q * go;
             }
         } else {
             gval = -g_here + amp;
@@ -192,25 +226,22 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
         // The population that streams into x along opp comes from the solid node x + c_ip: the
         // pull of the next step reads it from slot (opp, x + c_ip).
         const long long solid = (long long)x + cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
-        ST::st_f(fB + (long long)o * L + solid, (typename ST::R)fval, w, ph.t0);
-        ST::st_g(gB + (long long)o * L + solid, (typename ST::R)gval, w, ph.t0);
-        // In FP32/FP16 storage the value the reference would read back is the rounded one.
-        const double f_out = (MODE == RBTP_STORE_F64) ? fval
-                              : (double)ST::ld_f(fB + (long long)o * L + solid, w, ph.t0);
-        const double g_out = (MODE == RBTP_STORE_F64) ? gval
-                              : (double)ST::ld_g(gB + (long long)o * L + solid, w, ph.t0);
+        ST::st_f(fB + (long long)o * L + solid, fval, w, ph.t0);
+        ST::st_g(gB + (long long)o * L + solid, gval, w, ph.t0);
+        // In FP16 storage the value the reference would read back is the rounded one.
+        const RR f_out = (MODE != RBTP_STORE_F16S) ? fval : ST::ld_f(fB + (long long)o * L + solid, w, ph.t0);
+        const RR g_out = (MODE != RBTP_STORE_F16S) ? gval : ST::ld_g(gB + (long long)o * L + solid, w, ph.t0);
         // ibb.cu:160-187 (force, torque about the same intersection point) and 202-204 (heat)
-        const double rx = relx, ry = rely, rz = relz;
-        const double Fx = (cxi - uwx) * f_here - (-cxi - uwx) * f_out;
-        const double Fy = (cyi - uwy) * f_here - (-cyi - uwy) * f_out;
-        const double Fz = (czi - uwz) * f_here - (-czi - uwz) * f_out;
-        acc[0] += Fx;
-        acc[1] += Fy;
-        acc[2] += Fz;
-        acc[3] += ry * Fz - rz * Fy;
-        acc[4] += rz * Fx - rx * Fz;
-        acc[5] += rx * Fy - ry * Fx;
-        acc[6] += g_here - g_out;
+        const RR Fx = ((RR)cxi - uwx) * f_here - ((RR)-cxi - uwx) * f_out;
+        const RR Fy = ((RR)cyi - uwy) * f_here - ((RR)-cyi - uwy) * f_out;
+        const RR Fz = ((RR)czi - uwz) * f_here - ((RR)-czi - uwz) * f_out;
+        acc[0] += (double)Fx;
+        acc[1] += (double)Fy;
+        acc[2] += (double)Fz;
+        acc[3] += (double)(rely * Fz - relz * Fy);
+        acc[4] += (double)(relz * Fx - relx * Fz);
+        acc[5] += (double)(relx * Fy - rely * Fx);
+        acc[6] += (double)(g_here - g_out);
     }
     block_reduce_fixed<7, IBB_THREADS>(acc, sh);
     if (threadIdx.x == 0) {
@@ -461,15 +492,27 @@ __device__ __forceinline__ void mark_body(const Geo &geo, const Phys &ph, const 
     if (b.x0 > b.x1 || b.y0 > b.y1 || b.z0 > b.z1) return;
     const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
     const int total = nx * ny * nz;
+    // Single-precision classification away from the surface, the exact FP64 predicate in a band
+    // around it.  The band half-width bounds the float error of |x - X|^2 (coordinate rounding
+    // ~6e-8 |X| per component, arithmetic rounding ~1e-7 relative), so every node is classified
+    // exactly as the FP64 test classifies it.
+    const float pxf = (float)px, pyf = (float)py, pzf = (float)pz, rf2 = (float)rsq;
+    const float amax = fmaxf(fabsf(pxf), fmaxf(fabsf(pyf), fabsf(pzf)));
+    const float band = 1.0e-3f * rf2 + 1.0e-5f * (amax + 1.0f) * ((float)r + 2.0f) + 1.0e-3f;
     for (int t = threadIdx.x; t < total; t += blockDim.x) {
         const int lz = t / (nx * ny);
         const int rem = t - lz * nx * ny;
         const int ly = rem / nx;
         const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
-        const double dx = dsub((double)ix + 0.5, px);
-        const double dy = dsub((double)iy + 0.5, py);
-        const double dz = dsub((double)iz + 0.5, pz);
-        if (sq3(dx, dy, dz) > rsq) continue;
+        const float fx = ((float)ix + 0.5f) - pxf, fy = ((float)iy + 0.5f) - pyf, fz = ((float)iz + 0.5f) - pzf;
+        const float d2 = fx * fx + fy * fy + fz * fz;
+        if (d2 > rf2 + band) continue;
+        if (d2 >= rf2 - band) {
+            const double dx = dsub((double)ix + 0.5, px);
+            const double dy = dsub((double)iy + 0.5, py);
+            const double dz = dsub((double)iz + 0.5, pz);
+            if (sq3(dx, dy, dz) > rsq) continue;
+        }
         const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
         atomicMin(reinterpret_cast<unsigned int *>(owner) + idx, (unsigned int)p);
     }
@@ -514,6 +557,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total
     return wbase + incl - v;
 }
 
+template <bool F32Q>
 __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
                                                const int *owner, DevStatus *status, int p, int *wsum,
                                                int *cand /* (box-local node index << 5) | direction */)
@@ -580,8 +624,15 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
                 const int ly = rem / nx;
                 const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
                 node = (int)((long long)iz * geo.lxy + (long long)iy * geo.lx + ix);
-                ok = link_q(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (double)ix + 0.5, (double)iy + 0.5,
-                            (double)iz + 0.5, px, py, pz, rsq, q) ? 1 : 0;
+                int r32 = -1;
+                if constexpr (F32Q)
+                    r32 = link_q_f32(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (float)((double)ix + 0.5 - px),
+                                     (float)((double)iy + 0.5 - py), (float)((double)iz + 0.5 - pz),
+                                     (float)rsq, q);
+                if (r32 > 0) ok = 1;
+                else
+                    ok = link_q(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (double)ix + 0.5, (double)iy + 0.5,
+                                (double)iz + 0.5, px, py, pz, rsq, q) ? 1 : 0;
             }
             int ltotal;
             const int lpos = base + block_exclusive_scan(ok, wsum, ltotal);
@@ -601,13 +652,14 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
     if (threadIdx.x == 0) pb.link_cnt[p] = base;
 }
 
+template <bool F32Q>
 __global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const Phys ph,
                                                             const PartBuffers pb, const int *owner,
                                                             DevStatus *status)
 {
     __shared__ int wsum[LINK_THREADS / 32];
     __shared__ int cand[LINK_CAND];
-    link_fill_body(geo, ph, pb, owner, status, blockIdx.x, wsum, cand);
+    link_fill_body<F32Q>(geo, ph, pb, owner, status, blockIdx.x, wsum, cand);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -895,11 +947,12 @@ cudaError_t launch_initial_owner(const Geo &geo, const Phys &ph, const PartBuffe
     return launch_mark(geo, ph, pb, owner, st);
 }
 
-cudaError_t launch_link_fill(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+cudaError_t launch_link_fill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
                              const int *owner, DevStatus *status, cudaStream_t st)
 {
     if (pb.np <= 0) return cudaSuccess;
-    k_link_fill<<<pb.np, LINK_THREADS, 0, st>>>(geo, ph, pb, owner, status);
+    if (mode == RBTP_STORE_F64) k_link_fill<false><<<pb.np, LINK_THREADS, 0, st>>>(geo, ph, pb, owner, status);
+    else k_link_fill<true><<<pb.np, LINK_THREADS, 0, st>>>(geo, ph, pb, owner, status);
     return cudaGetLastError();
 }
 
@@ -1004,13 +1057,14 @@ __global__ void k_mark_b(const CavDesc *desc, const int2 *pmap)
     mark_body(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], mp.y);
 }
 
+template <bool F32Q>
 __global__ void __launch_bounds__(LINK_THREADS) k_link_fill_b(const CavDesc *desc, const int2 *pmap)
 {
     __shared__ int wsum[LINK_THREADS / 32];
     __shared__ int cand[LINK_CAND];
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
-    link_fill_body(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], d.status, mp.y, wsum, cand);
+    link_fill_body<F32Q>(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], d.status, mp.y, wsum, cand);
 }
 
 __global__ void k_new_fluid_b(const CavDesc *desc, const int2 *pmap)
@@ -1054,7 +1108,7 @@ cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int to
     k_update_b<<<bl, t, 0, st>>>(desc, pmap, total);
     k_owner_fill_b<<<dim3(64, npmem), 256, 0, st>>>(desc, pmem);
     k_mark_b<<<total, 256, 0, st>>>(desc, pmap);
-    k_link_fill_b<<<total, LINK_THREADS, 0, st>>>(desc, pmap);
+    k_link_fill_b<MODE != RBTP_STORE_F64><<<total, LINK_THREADS, 0, st>>>(desc, pmap);
     k_new_fluid_b<<<total, 256, 0, st>>>(desc, pmap);
     k_refill_compute_b<MODE><<<dim3(8, npmem), 256, 0, st>>>(desc, pmem);
     k_refill_scatter_b<MODE><<<dim3(8, npmem), 256, 0, st>>>(desc, pmem);

@@ -265,7 +265,7 @@ cudaError_t launch_contacts(const Geo &geo, const Phys &ph, const PartBuffers &p
 cudaError_t launch_update(const Phys &ph, const PartBuffers &pb, cudaStream_t st);
 cudaError_t launch_mark(const Geo &geo, const Phys &ph, const PartBuffers &pb, int *owner_out,
                         cudaStream_t st);
-cudaError_t launch_link_fill(const Geo &geo, const Phys &ph, const PartBuffers &pb,
+cudaError_t launch_link_fill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
                              const int *owner, DevStatus *status, cudaStream_t st);
 cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
                           const int *owner_prev, const int *owner_cur, void *f, void *g,
