@@ -19,6 +19,20 @@ CASES = {
                           rho_particle_ratio=1.0),
 }
 
+# Timing cases (oracle/ref_pin/time_ref.py): the benchmark workloads, 320x320x160 at Ra = 1e8,
+# single phase and with 1000 spheres of diameter 16 at density ratio 1.0.
+_V16 = 4.0 * math.pi * 8.0 ** 3 / 3.0
+TIMING = {
+    "ref_production": dict(lx=320, ly=320, lz=160, rayleigh=1.0e8, prandtl=0.71,
+                           visc=0.1414 * 320 * math.sqrt(0.71 / 1.0e8), activate_particles=0,
+                           particle_fraction=0.0, particle_diam_frac=1.0 / 20.0,
+                           rho_particle_ratio=1.0),
+    "ref_particle_laden": dict(lx=320, ly=320, lz=160, rayleigh=1.0e8, prandtl=0.71,
+                               visc=0.1414 * 320 * math.sqrt(0.71 / 1.0e8), activate_particles=1,
+                               particle_fraction=1000.5 * _V16 / (320 * 320 * 160),
+                               particle_diam_frac=16.0 / 320.0, rho_particle_ratio=1.0),
+}
+
 # parameters.h macros that are not case fields (reference defaults, parameters.h:4-53)
 FIXED = dict(continuous_steps=0, nend=1000000, ndiag=125, nflowout=25000, nnuout=125, nout_p=125,
              t_hot=1.0, t_cold=0.0, t_ref=0.5, beta=0.0000625, rho0=1.0, cp_particle_ratio=10.0,
@@ -29,7 +43,7 @@ FIXED = dict(continuous_steps=0, nend=1000000, ndiag=125, nflowout=25000, nnuout
 
 def values(case: str) -> dict:
     v = dict(FIXED)
-    v.update(CASES[case])
+    v.update(CASES[case] if case in CASES else TIMING[case])
     return v
 
 

@@ -12,7 +12,17 @@
 //   in_dir:  cfg.txt (key value lines), f.bin, g.bin, flow7.bin, particles.bin (np x 33, optional)
 //   out_dir: links0.bin owner0.bin (loaded state), f.bin g.bin macros.bin particles.bin owner.bin
 //            links.bin newfluid.bin (after nsteps)
+//
+// timing: ref_driver <cubin> <in_dir> time <warmup> <steps>
+//   Times the reference's per-step sequence (kernels and device-to-device copies exactly as its host
+//   loop issues them) on the seeded synthetic start that cfg.txt describes ("synthetic 1": f = 0,
+//   g = w_i T with T the linear profile plus the SplitMix64 perturbation of rbtp/workloads.py) and
+//   prints one line "ref_time ms_per_step <t> ms_per_step_with_host_scans <t2> ...".  The two
+//   prefix sums that the reference runs with CUB are host scans here; their time is excluded from
+//   the first figure (it counts only the reference's own device work and host loop).
 #include <cuda.h>
+
+#include <chrono>
 
 #include <cmath>
 #include <cstdio>
@@ -127,8 +137,16 @@ int num_links = 0, link_cap = 0, num_nf = 0, nf_cap = 0;
 
 void memcpy_dd(CUdeviceptr dst, CUdeviceptr src, size_t b) { CU(cuMemcpyDtoD(dst, src, b)); }
 
+double g_scan_seconds = 0.0;   // wall time spent in the host stand-ins for the CUB scans
+
 void host_scan(int n_total_last, int &total)
 {
+    CU(cuCtxSynchronize());
+    const auto t0 = std::chrono::steady_clock::now();
+    struct Clock {
+        std::chrono::steady_clock::time_point t0;
+        ~Clock() { g_scan_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+    } clk{t0};
     std::vector<int> cnt(L), off(L);
     CU(cuMemcpyDtoH(cnt.data(), d_count, L * sizeof(int)));
     long long run = 0;
@@ -280,13 +298,47 @@ void step()
     refill_nodes();
 }
 
-}  // namespace
-
-int main(int argc, char **argv)
+// SplitMix64 output k (k = 1..n) of the stream with the given seed, as doubles in [0, 1)
+// (rbtp/workloads.py splitmix64_uniform).
+double splitmix_uniform(unsigned long long seed, unsigned long long k)
 {
-    if (argc != 5) { std::fprintf(stderr, "usage: ref_driver <cubin> <in_dir> <nsteps> <out_dir>\n"); return 2; }
-    const std::string in = argv[2], out = argv[4];
-    const int nsteps = std::atoi(argv[3]);
+    unsigned long long z = seed + k * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z = z ^ (z >> 31);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// f = 0, g_i = w_i T, flow7 = (0, 0, 0, 0, T, 0, 0) with T the seeded linear-conduction start.
+void synthetic_state(std::vector<char> &f, std::vector<char> &g, std::vector<char> &f7)
+{
+    const size_t P = 27 * (size_t)L * 8, S = (size_t)L * 8;
+    f.assign(P, 0);
+    g.assign(P, 0);
+    f7.assign(7 * S, 0);
+    double *gp = (double *)g.data(), *tp7 = (double *)f7.data() + 4 * L;
+    const double th = cfg["t_hot"], tc = cfg["t_cold"], amp = cfg.count("amp") ? cfg["amp"] : 1e-3;
+    const unsigned long long seed = (unsigned long long)cfg["seed"];
+    const double w[4] = {8.0 / 27.0, 2.0 / 27.0, 1.0 / 54.0, 1.0 / 216.0};
+    for (long long n = 0; n < L; ++n) {
+        const int x = (int)(n % LX);
+        double T = th - (x + 0.5) / LX * (th - tc);
+        T = T + amp * (2.0 * splitmix_uniform(seed, (unsigned long long)n + 1) - 1.0);
+        tp7[n] = T;
+        for (int i = 0; i < 27; ++i) gp[(size_t)i * L + n] = w[i == 0 ? 0 : (i <= 6 ? 1 : (i <= 18 ? 2 : 3))] * T;
+    }
+}
+
+int run(int argc, char **argv)
+{
+    const bool timing = argc == 6 && std::string(argv[3]) == "time";
+    if (argc != 5 && !timing) {
+        std::fprintf(stderr, "usage: ref_driver <cubin> <in_dir> <nsteps> <out_dir>\n"
+                             "       ref_driver <cubin> <in_dir> time <warmup> <steps>\n");
+        return 2;
+    }
+    const std::string in = argv[2], out = timing ? std::string() : std::string(argv[4]);
+    const int nsteps = timing ? 0 : std::atoi(argv[3]);
     {
         std::ifstream cf(in + "/cfg.txt");
         std::string k;
@@ -337,7 +389,9 @@ int main(int argc, char **argv)
     d_ptemp = dalloc(PB); d_pheat = dalloc(PB); d_pheat_prev = dalloc(PB);
 
     // load_restart_state (initial.cu:194-236)
-    auto f = slurp(in + "/f.bin"), g = slurp(in + "/g.bin"), f7 = slurp(in + "/flow7.bin");
+    std::vector<char> f, g, f7;
+    if (cfg.count("synthetic") && cfg["synthetic"] != 0.0) synthetic_state(f, g, f7);
+    else { f = slurp(in + "/f.bin"); g = slurp(in + "/g.bin"); f7 = slurp(in + "/flow7.bin"); }
     if (f.size() != P || g.size() != P || f7.size() != 7 * S) { std::fprintf(stderr, "bad input sizes\n"); return 2; }
     CU(cuMemcpyHtoD(d_f, f.data(), P));
     CU(cuMemcpyHtoD(d_g, g.data(), P));
@@ -369,6 +423,23 @@ int main(int argc, char **argv)
         memcpy_dd(d_owner_prev, d_owner, L * 4);
     }
     CU(cuCtxSynchronize());
+    if (timing) {
+        f.clear(); f.shrink_to_fit(); g.clear(); g.shrink_to_fit();
+        const int warm = std::atoi(argv[4]), steps = std::atoi(argv[5]);
+        for (int s = 0; s < warm; ++s) step();
+        CU(cuCtxSynchronize());
+        g_scan_seconds = 0.0;
+        const auto t0 = std::chrono::steady_clock::now();
+        for (int s = 0; s < steps; ++s) step();
+        CU(cuCtxSynchronize());
+        const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        std::printf("ref_time ms_per_step %.6f ms_per_step_with_host_scans %.6f steps %d warmup %d nodes %lld "
+                    "npart %d links %d\n", 1e3 * (sec - g_scan_seconds) / steps, 1e3 * sec / steps, steps, warm,
+                    L, NP, num_links);
+        CU(cuModuleUnload(mod));
+        CU(cuDevicePrimaryCtxRelease(dev));
+        return 0;
+    }
     // the link set of the loaded state
     {
         std::vector<Link> lk(num_links);
@@ -426,3 +497,7 @@ int main(int argc, char **argv)
     std::printf("ref_driver: %d steps, %d links, %d new-fluid nodes\n", nsteps, num_links, num_nf);
     return 0;
 }
+
+}  // namespace
+
+int main(int argc, char **argv) { return run(argc, argv); }
