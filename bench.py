@@ -228,49 +228,92 @@ def batch_variant(torch, steps: int, warmup: int, n: int = 256) -> dict:
     return out
 
 
-def serving_variant(n: int = 16, rate: float = 4.0, seed: int = 3, tick: int = 250,
-                    batched_mlups=None) -> dict:
-    """Serving: n solve requests drawn like the batched ensemble (sizes, Ra, Pr, spheres) with
-    horizons uniform in [2000, 50000] steps and Nu sampled every 500 steps, arriving as a Poisson
-    stream of the given rate (requests/s), admitted by footprint within 180 GB, FP32 storage.
-    Latency = completion - scheduled arrival (server clock)."""
+def _stream(cfgs, horizons, arrivals, tick: int, every: int = 500) -> dict:
+    """One Poisson stream through a fresh server; latency = completion - scheduled arrival."""
     import numpy as np
-    from rbtp import Server, workloads as W
-    rng = np.random.default_rng(seed)
-    cfgs = W.ensemble(n, seed=seed, storage=1)
-    horizons = rng.integers(2000, 50001, size=n)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    from rbtp import Server
+    n = len(cfgs)
     srv = Server(1, hbm_budget=180e9)
     t0 = srv.stats()["clock"]
-    ids, k, peak = [], 0, 0
+    ids, k, peak, trace = [], 0, 0, []
     while True:
         now = srv.stats()["clock"] - t0
         while k < n and arrivals[k] <= now:
-            ids.append(srv.submit(cfgs[k], int(horizons[k]), 500))
+            ids.append(srv.submit(cfgs[k], int(horizons[k]), every))
             k += 1
         a, q = srv.tick(tick)
         peak = max(peak, a)
+        st = srv.stats()
+        trace.append((st["clock"] - t0, st["node_updates"]))
         if k == n and a == 0 and q == 0:
             break
         if a == 0 and q == 0 and k < n:
             time.sleep(max(0.0, min(0.05, arrivals[k] - (srv.stats()["clock"] - t0))))
     st = srv.stats()
-    lat, ok = [], 0
+    lat, ok, failed = [], 0, {}
     for i, rid in enumerate(ids):
         p = srv.poll(rid)
         _, _, done = srv.times(rid)
         if p["state"] == Server.DONE:
             ok += 1
             lat.append(done - t0 - arrivals[i])
-    span = st["clock"] - t0 - arrivals[0]
-    served = st["node_updates"] / span / 1e6
-    out = {"requests": n, "completed": ok, "rate_per_s": rate, "tick_steps": tick,
-           "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
-           "served_mlups": served, "peak_active": peak, "makespan_s": round(span, 3),
-           "node_updates": st["node_updates"]}
-    if batched_mlups:
-        out["served_over_batched"] = served / batched_mlups
+        else:
+            failed[str(i)] = p["status"]
     srv.close()
+    span = st["clock"] - t0 - arrivals[0]
+    # node updates up to the last arrival (the stream is still feeding the server then)
+    t_last = arrivals[-1]
+    upd_last = max([u for t, u in trace if t <= t_last] or [0.0])
+    t_at = max([t for t, u in trace if t <= t_last] or [arrivals[0]])
+    return {"rate_per_s": float(n / arrivals[-1]) if arrivals[-1] > 0 else None,
+            "completed": ok, "failed_status": failed,
+            "latency_p50_s": float(np.percentile(lat, 50)) if lat else None,
+            "latency_p99_s": float(np.percentile(lat, 99)) if lat else None,
+            "served_mlups": st["node_updates"] / span / 1e6,
+            "served_mlups_until_last_arrival": (upd_last / (t_at - arrivals[0]) / 1e6
+                                                if t_at > arrivals[0] else None),
+            "peak_active": peak, "makespan_s": round(span, 3), "ticks": len(trace),
+            "node_updates": st["node_updates"]}
+
+
+def serving_variant(n: int = 16, rates=(0.5, 4.0), seed: int = 3, tick: int = 250,
+                    batched_mlups=None) -> dict:
+    """Serving: n solve requests drawn like the batched ensemble (sizes, Ra, Pr, spheres) with
+    horizons uniform in [2000, 50000] steps and Nu sampled every 500 steps, arriving as a Poisson
+    stream (the same requests at each swept rate, requests/s), admitted by footprint within 180 GB,
+    FP32 storage.  Beside it: the same requests solved one after another by the plain FP64 path,
+    estimated from 100 timed steps of each (after 10 warm-up steps) times its horizon."""
+    import numpy as np
+    from rbtp import Solver, workloads as W
+    rng = np.random.default_rng(seed)
+    cfgs = W.ensemble(n, seed=seed, storage=1)
+    horizons = rng.integers(2000, 50001, size=n)
+    gaps = rng.exponential(1.0, size=n)
+    streams = {}
+    for rate in rates:
+        streams[str(rate)] = _stream(cfgs, horizons, np.cumsum(gaps / rate), tick)
+    # sequential plain FP64 solves of the same requests
+    seq_s, work = 0.0, 0.0
+    for c, h in zip(W.ensemble(n, seed=seed, storage=0), horizons):
+        s = Solver(c)
+        s.initialize()
+        s.step(10)
+        s.synchronize()
+        t0 = time.perf_counter()
+        s.step(100)
+        s.synchronize()
+        seq_s += (time.perf_counter() - t0) / 100 * int(h)
+        work += float(c.nodes) * int(h)
+        s.close()
+    top = streams[str(max(rates))]
+    out = {"requests": n, "tick_steps": tick, "sample_every": 500, "horizons": "uniform 2000..50000",
+           "streams": streams, "latency_p50_s": top["latency_p50_s"], "latency_p99_s": top["latency_p99_s"],
+           "served_mlups": top["served_mlups"], "completed": top["completed"],
+           "sequential_fp64_mlups": work / seq_s / 1e6,
+           "sequential_fp64_makespan_s": round(seq_s, 1)}
+    out["served_over_sequential_fp64"] = top["served_mlups"] / out["sequential_fp64_mlups"]
+    if batched_mlups:
+        out["served_over_batched"] = top["served_mlups"] / batched_mlups
     return out
 
 
@@ -335,9 +378,11 @@ def _barrier(dist):
 
 
 def _max_over_ranks(torch, dist, v):
+    """The largest of the ranks' values (the slowest replica sets the step time)."""
     if dist is None:
         return v
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

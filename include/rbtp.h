@@ -196,6 +196,14 @@ int  rbtp_write_flow(rbtp_handle *h, const char *dir, int istep);        /* outp
 int  rbtp_write_fg(rbtp_handle *h, const char *dir, int istep);          /* output_fg     */
 int  rbtp_write_particles(rbtp_handle *h, const char *dir, int istep);   /* output_particles */
 
+/* Exact checkpoint of the whole step state in the handle's storage precision (populations of the
+ * current buffer, F_x auxiliary, wall densities, current macroscopic fields, particle columns);
+ * rbtp_checkpoint_read into a handle created from the same configuration resumes the run bit for
+ * bit.  No counterpart in the reference (its restart files, rbtp_load_restart, hold the exported
+ * FP64 populations and %14.6e particle text). */
+int  rbtp_checkpoint_write(rbtp_handle *h, const char *path);
+int  rbtp_checkpoint_read(rbtp_handle *h, const char *path);
+
 /* ---- batched execution (spec addition: many cavities, one persistent launch) ---------- */
 /* A batch advances many independent cavities (own sizes, Ra, Pr, particle counts; one storage
  * mode) in lockstep: per step ONE persistent launch of the fused step over a packed tile table of all
@@ -218,10 +226,24 @@ int  rbtp_batch_create(int storage, rbtp_batch **out);
 int  rbtp_batch_destroy(rbtp_batch *b);
 int  rbtp_batch_add(rbtp_batch *b, rbtp_handle *h);
 int  rbtp_batch_remove(rbtp_batch *b, rbtp_handle *h);
-/* Materialise h's macroscopic fields every `every` steps (0 = only its cfg cadence): the sampling
- * that a serving loop uses for Nu time series. */
+/* Sample h every `every` steps (0 = only at its stop step): the step materialises the macroscopic
+ * fields and ends with an on-device plane-sum reduction written into h's sample ring (64 slots), so
+ * batch calls need not end on sample steps.  rbtp_batch_samples turns ring slots into Nu rows. */
 int  rbtp_batch_set_sampling(rbtp_batch *b, rbtp_handle *h, int every);
+/* h stops advancing once its step counter reaches stop_step (<= 0: never); the other members keep
+ * going, so batch calls need not end on any member's horizon. */
+int  rbtp_batch_set_stop(rbtp_batch *b, rbtp_handle *h, int stop_step);
+/* The Nu rows (output_nu's formulas, rbtp_nu_row; step = the member's step of the sample) of up to
+ * cap samples taken since the last call, oldest first.  RBTP_ERR_CAPACITY if more than 64 samples
+ * were taken between two calls (the oldest are lost). */
+int  rbtp_batch_samples(rbtp_batch *b, rbtp_handle *h, rbtp_nu_row *rows, int cap, int *nrows);
 int  rbtp_batch_step(rbtp_batch *b, int nsteps);
+/* rbtp_batch_step in two halves: launch returns with the steps in flight (the batch stream works
+ * while the caller prepares new members); wait ends them and updates every member.  In between,
+ * calls on the batch or its members return RBTP_ERR_STATE (rbtp_batch_remove and rbtp_destroy
+ * wait first). */
+int  rbtp_batch_launch(rbtp_batch *b, int nsteps);
+int  rbtp_batch_wait(rbtp_batch *b);
 int  rbtp_batch_stats_get(rbtp_batch *b, rbtp_batch_stats *out);
 /* Force a tile shape (0/1) and persistent grid (blocks), or re-enable the autotuner with shape -1. */
 int  rbtp_batch_set_launch(rbtp_batch *b, int shape, int grid);
@@ -230,12 +252,14 @@ int  rbtp_batch_set_launch(rbtp_batch *b, int shape, int grid);
 int  rbtp_footprint(const rbtp_config *cfg, size_t *bytes);
 
 /* ---- continuous-batching solve server (spec addition) ------------------------------------ */
-/* Requests (case, horizon in steps, Nu sampling cadence) are queued from any thread; each tick
- * admits queued requests in arrival order while their footprint fits the HBM budget (and the
- * active-slot limit, 0 = none), advances all active requests together in one batch by as many steps
- * as none of them needs to stop for (at most max_steps), appends a Nu row (rbtp_nu_row, step =
- * the request's own step) at each request's sample steps and at its last step, and retires finished
- * requests.  State stays resident between ticks; results do not depend on the other requests. */
+/* Requests (case, horizon in steps, Nu sampling cadence) are queued from any thread.  Each tick
+ * launches max_steps steps of the batch of active requests (bounded by the longest remaining
+ * horizon and the sample-ring capacity; each request stops on the device at its own horizon and
+ * samples on its own cadence), and while they run prepares queued requests in arrival order whose
+ * footprint fits the HBM budget (and the active-slot limit, 0 = none): allocation and fresh start.
+ * After the steps it appends the Nu rows (rbtp_nu_row, step = the request's own step) of each
+ * request's samples and of its last step, retires finished requests and lets the prepared ones
+ * join.  State stays resident between ticks; results do not depend on the other requests. */
 typedef struct rbtp_server rbtp_server;
 #define RBTP_REQ_QUEUED 0
 #define RBTP_REQ_ACTIVE 1
@@ -253,6 +277,12 @@ int  rbtp_server_poll(rbtp_server *s, int id, int *state, int *steps_done, rbtp_
 int  rbtp_server_request_times(rbtp_server *s, int id, double *t_submit, double *t_admit, double *t_done);
 int  rbtp_server_stats(rbtp_server *s, double *node_updates, double *steps, double *used_bytes,
                        double *clock);
+/* Checkpoint between ticks into an existing directory (server.bin + req_<id>.ckp per active
+ * request, exact), and restore into a freshly created server: queued requests are re-queued in
+ * order, active requests resume from their checkpoints bit for bit, finished ones keep their
+ * series, and the server clock continues.  No counterpart in the reference. */
+int  rbtp_server_checkpoint(rbtp_server *s, const char *dir);
+int  rbtp_server_restore(rbtp_server *s, const char *dir);
 
 /* ---- allocation-free diagnostic sums ----------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory — code hosted in

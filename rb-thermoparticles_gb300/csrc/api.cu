@@ -23,6 +23,7 @@
 
 using namespace rbtp;
 constexpr int NP_COLS = RBTP_PARTICLE_COLS;
+constexpr char POS_MAGIC[9] = "RBTPPOS1";   // exact particle sidecar pos_%09d.bin
 
 namespace {
 
@@ -107,6 +108,7 @@ int upload_particles(rbtp_handle *h, const double *rows)
 int check_ready(rbtp_handle *h)
 {
     if (!h) return RBTP_ERR_ARG;
+    if (rbtp_batch_busy(h)) return fail(h, RBTP_ERR_STATE, "the handle's batch has steps in flight (rbtp_batch_wait)");
     if (!h->initialised) return fail(h, RBTP_ERR_STATE, "state not initialised (call rbtp_init_fresh or rbtp_load_state)");
     return RBTP_OK;
 }
@@ -209,7 +211,7 @@ int rbtp_footprint(const rbtp_config *cfg, size_t *bytes)
     const int np = cfg->activate_particles ? d.npart : 0;
     if (np > 0) {
         const double r = d.particle_radius;
-        b += (size_t)np * (NP_COLS + 10) * sizeof(double);   // state, hF, hT, hQ, cF
+        b += (size_t)np * (NP_COLS + 7 * IBB_CHUNKS + 3) * sizeof(double);   // state, IBB partials, cF
         b += 2 * L * sizeof(int);                             // owner maps
         const size_t lcap = (size_t)std::min<long long>(26 * shell_bound(r, r + std::sqrt(3.0)), 1LL << 30);
         b += (size_t)np * lcap * (2 * sizeof(int) + sizeof(double)) + np * sizeof(int);
@@ -300,8 +302,7 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
         const double r = h->der.particle_radius;
         CKC(dalloc(&pb.state, (size_t)np * NP_COLS));
         CKC(cudaMemsetAsync(pb.state, 0, (size_t)np * NP_COLS * sizeof(double), h->stream));
-        CKC(dalloc(&pb.hF, 3 * (size_t)np)); CKC(dalloc(&pb.hT, 3 * (size_t)np));
-        CKC(dalloc(&pb.hQ, (size_t)np)); CKC(dalloc(&pb.cF, 3 * (size_t)np));
+        CKC(dalloc(&pb.hpart, (size_t)IBB_CHUNKS * 7 * np)); CKC(dalloc(&pb.cF, 3 * (size_t)np));
         CKC(dalloc(&h->owner[0], L)); CKC(dalloc(&h->owner[1], L));
         CKC(cudaMemsetAsync(h->owner[0], 0xFF, L * sizeof(int), h->stream));
         CKC(cudaMemsetAsync(h->owner[1], 0xFF, L * sizeof(int), h->stream));
@@ -348,9 +349,9 @@ int rbtp_destroy(rbtp_handle *h)
     cudaFree(h->rho); cudaFree(h->ux); cudaFree(h->uy); cudaFree(h->uz); cudaFree(h->phi);
     cudaFree(h->ted); cudaFree(h->ked); cudaFree(h->fcol); cudaFree(h->gcol);
     cudaFree(h->status); if (h->status_host) cudaFreeHost(h->status_host);
-    cudaFree(h->partials); cudaFree(h->plane);
+    cudaFree(h->partials); cudaFree(h->plane); cudaFree(h->ring);
     PartBuffers &pb = h->pb;
-    cudaFree(pb.state); cudaFree(pb.hF); cudaFree(pb.hT); cudaFree(pb.hQ); cudaFree(pb.cF);
+    cudaFree(pb.state); cudaFree(pb.hpart); cudaFree(pb.cF);
     cudaFree(pb.link_node); cudaFree(pb.link_dir); cudaFree(pb.link_q); cudaFree(pb.link_cnt);
     cudaFree(pb.nf_node); cudaFree(pb.nf_pid); cudaFree(pb.nf_val); cudaFree(pb.nf_mac);
     cudaFree(pb.cell_count); cudaFree(pb.cell_start); cudaFree(pb.cell_fill); cudaFree(pb.cell_items);
@@ -439,6 +440,7 @@ int rbtp_init_fresh(rbtp_handle *h)
     h->phase = PHASE_HOME;
     h->ocur = 0;
     CK(cudaMemsetAsync(h->status, 0, sizeof(DevStatus), h->stream));
+    h->ring_drained = 0;
     if (np > 0) {
         int s = build_links(h, h->owner[0]);  // initial flags == flags of build_links
         if (s) return s;
@@ -467,6 +469,7 @@ int rbtp_load_state(rbtp_handle *h, const double *f, const double *g, const doub
     h->phase = PHASE_HOME;
     h->ocur = 0;
     CK(cudaMemsetAsync(h->status, 0, sizeof(DevStatus), h->stream));
+    h->ring_drained = 0;
     if (np > 0) {
         s = upload_particles(h, particles);
         if (s) return s;
@@ -719,8 +722,15 @@ int rbtp_nu(rbtp_handle *h, int istep, rbtp_nu_row *row)
     if (!h->macros_valid) return fail(h, RBTP_ERR_STATE, "macroscopic fields were not materialised on the last step");
     s = plane_sums(h);
     if (s) return s;
+    return nu_from_planes(h, h->plane_host.data(), istep, row);
+}
+
+}  // extern "C"
+
+// output_statis.cu:111-223
+int rbtp::nu_from_planes(rbtp_handle *h, const double *pl, int istep, rbtp_nu_row *row)
+{
     const int lx = h->geo.lx;
-    const double *pl = h->plane_host.data();
     const double vf = h->cfg.particle_fraction;
     const double ff = std::fmax(0.0, 1.0 - vf);
     double avg_f = 0.0, avg_p = 0.0, bottom = 0.0, top = 0.0, bc = 0.0, tc = 0.0;
@@ -753,6 +763,8 @@ int rbtp_nu(rbtp_handle *h, int istep, rbtp_nu_row *row)
         return fail(h, RBTP_ERR_NONFINITE, "non-finite Nusselt number");
     return RBTP_OK;
 }
+
+extern "C" {
 
 // output_statis.cu:64-109
 int rbtp_means(rbtp_handle *h, double means[4])
@@ -982,7 +994,16 @@ int rbtp_write_particles(rbtp_handle *h, const char *dir, int istep)
         for (int k = 0; k < NP_COLS; ++k) std::fprintf(fp, k + 1 < NP_COLS ? "%14.6e " : "%14.6e\n", c[k]);
     }
     std::fclose(fp);
-    return RBTP_OK;
+    // Exact sidecar (no counterpart in the reference, whose %14.6e text keeps 7 digits): the same
+    // rows as raw doubles, preferred by rbtp_load_restart so that a restart continues bit for bit.
+    std::snprintf(name, sizeof(name), "%s/pos/pos_%09d.bin", d.c_str(), istep);
+    fp = std::fopen(name, "wb");
+    if (!fp) return fail(h, RBTP_ERR_IO, std::string("cannot open ") + name);
+    const int hdr[2] = {np, NP_COLS};
+    const bool ok = std::fwrite(POS_MAGIC, 1, 8, fp) == 8 && std::fwrite(hdr, sizeof(int), 2, fp) == 2 &&
+                    std::fwrite(prow.data(), sizeof(double), prow.size(), fp) == prow.size();
+    std::fclose(fp);
+    return ok ? RBTP_OK : fail(h, RBTP_ERR_IO, std::string("short write: ") + name);
 }
 
 // load_restart_state (initial.cu:194-236) from the reference's files
@@ -1008,7 +1029,21 @@ int rbtp_load_restart(rbtp_handle *h, const char *dir, int step)
     if (r7 != 7 * L) return fail(h, RBTP_ERR_IO, std::string("flow restart file is short: ") + name);
     std::vector<double> prow;
     const int np = h->pb.np;
+    bool exact = false;
     if (np > 0) {
+        std::snprintf(name, sizeof(name), "%s/pos/pos_%09d.bin", d.c_str(), step);
+        if (FILE *bf = std::fopen(name, "rb")) {
+            char magic[8];
+            int hdr[2] = {0, 0};
+            prow.assign((size_t)np * NP_COLS, 0.0);
+            exact = std::fread(magic, 1, 8, bf) == 8 && std::memcmp(magic, POS_MAGIC, 8) == 0 &&
+                    std::fread(hdr, sizeof(int), 2, bf) == 2 && hdr[0] == np && hdr[1] == NP_COLS &&
+                    std::fread(prow.data(), sizeof(double), prow.size(), bf) == prow.size();
+            std::fclose(bf);
+            if (!exact) return fail(h, RBTP_ERR_IO, std::string("particle sidecar is corrupted or for another case: ") + name);
+        }
+    }
+    if (np > 0 && !exact) {
         std::snprintf(name, sizeof(name), "%s/pos/pos_%09d.txt", d.c_str(), step);
         std::ifstream in(name);
         if (!in) return fail(h, RBTP_ERR_IO, std::string("cannot open restart particle file ") + name);
@@ -1029,6 +1064,127 @@ int rbtp_load_restart(rbtp_handle *h, const char *dir, int step)
     h->cfg.continuous_steps = saved;
     if (s == RBTP_OK) h->istep = step;
     return s;
+}
+
+// Exact checkpoint of a handle's whole step state in its storage precision: the populations as
+// they sit in the current buffer (post-collision with the IBB/refill fix-ups, or at home after a
+// load), the F_x auxiliary, the wall densities of the Dirichlet image, the macroscopic fields when
+// they are current, and the 33 particle columns.  Solid flags and link slabs are rebuilt from the
+// positions on load (deterministically, as at the end of every step), so a run resumed from a
+// checkpoint continues bit for bit.  No counterpart in the reference.
+namespace {
+constexpr char CKP_MAGIC[9] = "RBTPCKP1";
+struct CkpHeader {
+    int version, mode, lx, ly, lz, np, phase, istep, macros_valid, pad;
+};
+size_t elem_bytes(int mode) { return mode == RBTP_STORE_F64 ? 8 : (mode == RBTP_STORE_F32 ? 4 : 2); }
+}  // namespace
+
+int rbtp_checkpoint_write(rbtp_handle *h, const char *path)
+{
+    int s = check_ready(h);
+    if (s) return s;
+    if (!path) return fail(h, RBTP_ERR_ARG, "path is null");
+    const size_t L = (size_t)h->geo.L, P = 27 * L * elem_bytes(h->mode), W = 2 * (size_t)h->geo.ly * h->geo.lz;
+    const int np = h->pb.np;
+    CkpHeader hd{1, h->mode, h->geo.lx, h->geo.ly, h->geo.lz, np, h->phase, h->istep, h->macros_valid ? 1 : 0, 0};
+    std::vector<char> pop(P);
+    std::vector<double> aux(L), wall(W), mac(h->macros_valid ? 5 * L : 0), prow((size_t)np * NP_COLS);
+    CK(cudaStreamSynchronize(h->stream));
+    FILE *fp = std::fopen(path, "wb");
+    if (!fp) return fail(h, RBTP_ERR_IO, std::string("cannot open ") + path);
+    bool ok = std::fwrite(CKP_MAGIC, 1, 8, fp) == 8 && std::fwrite(&hd, sizeof(hd), 1, fp) == 1 &&
+              std::fwrite(&h->cfg, sizeof(rbtp_config), 1, fp) == 1;
+    for (int k = 0; ok && k < 2; ++k) {
+        if (cudaMemcpy(pop.data(), k == 0 ? h->f[h->cur] : h->g[h->cur], P, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            std::fclose(fp);
+            return fail(h, RBTP_ERR_CUDA, "checkpoint read-back failed");
+        }
+        ok = std::fwrite(pop.data(), 1, P, fp) == P;
+    }
+    if (cudaMemcpy(aux.data(), h->faux, L * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(wall.data(), h->rho_wall, W * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        std::fclose(fp);
+        return fail(h, RBTP_ERR_CUDA, "checkpoint read-back failed");
+    }
+    if (h->macros_valid) {
+        const double *srcs[5] = {h->rho, h->ux, h->uy, h->uz, h->phi};
+        for (int k = 0; k < 5; ++k)
+            if (cudaMemcpy(&mac[k * L], srcs[k], L * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+                std::fclose(fp);
+                return fail(h, RBTP_ERR_CUDA, "checkpoint read-back failed");
+            }
+    }
+    if (np > 0 && (s = rbtp_get_particles(h, prow.data()))) {
+        std::fclose(fp);
+        return s;
+    }
+    ok = ok && std::fwrite(aux.data(), sizeof(double), L, fp) == L &&
+         std::fwrite(wall.data(), sizeof(double), W, fp) == W &&
+         std::fwrite(mac.data(), sizeof(double), mac.size(), fp) == mac.size() &&
+         std::fwrite(prow.data(), sizeof(double), prow.size(), fp) == prow.size();
+    ok = (std::fclose(fp) == 0) && ok;
+    return ok ? RBTP_OK : fail(h, RBTP_ERR_IO, std::string("short write: ") + path);
+}
+
+int rbtp_checkpoint_read(rbtp_handle *h, const char *path)
+{
+    if (!h || !path) return RBTP_ERR_ARG;
+    if (rbtp_batch_busy(h)) return fail(h, RBTP_ERR_STATE, "the handle's batch has steps in flight (rbtp_batch_wait)");
+    FILE *fp = std::fopen(path, "rb");
+    if (!fp) return fail(h, RBTP_ERR_IO, std::string("cannot open checkpoint ") + path);
+    char magic[8];
+    CkpHeader hd{};
+    rbtp_config saved;
+    const bool head = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, CKP_MAGIC, 8) == 0 &&
+                      std::fread(&hd, sizeof(hd), 1, fp) == 1 && std::fread(&saved, sizeof(saved), 1, fp) == 1;
+    if (!head || hd.version != 1) {
+        std::fclose(fp);
+        return fail(h, RBTP_ERR_IO, std::string("not a checkpoint file: ") + path);
+    }
+    if (hd.mode != h->mode || hd.lx != h->geo.lx || hd.ly != h->geo.ly || hd.lz != h->geo.lz || hd.np != h->pb.np) {
+        std::fclose(fp);
+        return fail(h, RBTP_ERR_CONFIG, "checkpoint was written for another grid, storage mode or particle count");
+    }
+    const size_t L = (size_t)h->geo.L, P = 27 * L * elem_bytes(h->mode), W = 2 * (size_t)h->geo.ly * h->geo.lz;
+    const int np = h->pb.np;
+    std::vector<char> f(P), g(P);
+    std::vector<double> aux(L), wall(W), mac(hd.macros_valid ? 5 * L : 0), prow((size_t)np * NP_COLS);
+    const bool body = std::fread(f.data(), 1, P, fp) == P && std::fread(g.data(), 1, P, fp) == P &&
+                      std::fread(aux.data(), sizeof(double), L, fp) == L &&
+                      std::fread(wall.data(), sizeof(double), W, fp) == W &&
+                      std::fread(mac.data(), sizeof(double), mac.size(), fp) == mac.size() &&
+                      std::fread(prow.data(), sizeof(double), prow.size(), fp) == prow.size();
+    std::fclose(fp);
+    if (!body) return fail(h, RBTP_ERR_IO, std::string("checkpoint is truncated: ") + path);
+    CK(cudaMemcpyAsync(h->f[0], f.data(), P, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->g[0], g.data(), P, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->faux, aux.data(), L * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->rho_wall, wall.data(), W * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    if (hd.macros_valid) {
+        double *dst[5] = {h->rho, h->ux, h->uy, h->uz, h->phi};
+        for (int k = 0; k < 5; ++k)
+            CK(cudaMemcpyAsync(dst[k], &mac[k * L], L * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    }
+    h->cur = 0;
+    h->phase = hd.phase == PHASE_COLLIDED ? PHASE_COLLIDED : PHASE_HOME;
+    h->ocur = 0;
+    CK(cudaMemsetAsync(h->status, 0, sizeof(DevStatus), h->stream));
+    h->ring_drained = 0;
+    if (np > 0) {
+        int s = upload_particles(h, prow.data());
+        if (s) return s;
+        s = build_links(h, h->owner[0]);
+        if (s) return s;
+    }
+    h->pb.owner_cur = h->owner[0];
+    CK(cudaStreamSynchronize(h->stream));   // host staging buffers go out of scope
+    h->istep = hd.istep;
+    h->initialised = true;
+    h->macros_valid = hd.macros_valid != 0;
+    h->dissip_valid = false;
+    h->plane_valid = false;
+    return read_status(h);
 }
 
 }  // extern "C"

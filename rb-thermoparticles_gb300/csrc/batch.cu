@@ -8,6 +8,12 @@
 // captured once into a CUDA graph and replayed for every step.  The autotuner times the candidate
 // (tile shape, persistent grid) pairs on the first steps of the batch — all candidates compute the
 // same values, so tuning steps are ordinary steps — and keeps the fastest.
+//
+// For continuous batching each member may carry a stop step (it goes idle there while the others
+// keep going: no batch call has to end on any member's horizon) and a sample ring (the step ends
+// with an on-device plane-sum reduction on the member's sampling cadence, so no batch call has to
+// end on a sample step either; the host turns ring slots into Nu rows later).  rbtp_batch_launch
+// returns with the steps in flight so the caller can prepare the next members meanwhile.
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -42,8 +48,15 @@ struct rbtp_batch {
     bool graph_valid = false;
     double last_ms = 0.0;
     double nodes = 0.0;
+    // asynchronous launch
+    bool inflight = false;
+    int inflight_steps = 0;
+    bool inflight_timed = false;
     std::string err;
 };
+
+// Slots of a member's sample ring.
+constexpr int RING_SLOTS = 64;
 
 namespace {
 
@@ -156,6 +169,13 @@ int refresh(rbtp_batch *b)
         d.ndiag = h->cfg.ndiag; d.nnuout = h->cfg.nnuout; d.nflowout = h->cfg.nflowout; d.nend = h->cfg.nend;
         d.every = h->sample_every;
         d.mode = h->mode;
+        d.last_out = h->macros_valid ? OUT_MACROS : OUT_NONE;
+        d.stop_at = h->stop_at;
+        d.samp_now = 0;
+        d.samp = h->ring;
+        d.samp_cap = h->ring_cap;
+        d.nchunks = h->nchunks;
+        d.partials = h->partials;
         BCK(cudaStreamSynchronize(h->stream));
     }
     BCK(cudaMemcpyAsync(b->d_desc, b->h_desc, (size_t)n * sizeof(CavDesc), cudaMemcpyHostToDevice, b->stream));
@@ -171,7 +191,8 @@ cudaError_t enqueue_step(rbtp_batch *b, int shape, int grid)
         return e;
     if ((e = launch_particles_batched(b->mode, b->d_desc, b->d_pmap, b->total_np, b->d_pmem, b->npmem, b->stream)))
         return e;
-    return launch_batch_advance(b->d_desc, n, b->stream);
+    if ((e = launch_batch_advance(b->d_desc, n, b->stream))) return e;
+    return launch_batch_sample(b->d_desc, n, b->stream);
 }
 
 int capture(rbtp_batch *b)
@@ -210,7 +231,7 @@ int sync_back(rbtp_batch *b)
         h->phase = d.phase ? PHASE_COLLIDED : PHASE_HOME;
         h->istep = d.istep;
         h->pb.owner_cur = h->owner[h->ocur];
-        h->macros_valid = d.out == OUT_MACROS;
+        h->macros_valid = d.last_out == OUT_MACROS;
         h->dissip_valid = false;
         h->plane_valid = false;
         const DevStatus &s = *h->status_host;
@@ -257,6 +278,7 @@ int rbtp_batch_create(int storage, rbtp_batch **out)
 int rbtp_batch_destroy(rbtp_batch *b)
 {
     if (!b) return RBTP_OK;
+    if (b->inflight) rbtp_batch_wait(b);
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (rbtp_handle *h : b->members) h->batch = nullptr;
     drop_graph(b);
@@ -275,6 +297,7 @@ int rbtp_batch_destroy(rbtp_batch *b)
 int rbtp_batch_add(rbtp_batch *b, rbtp_handle *h)
 {
     if (!b || !h) return RBTP_ERR_ARG;
+    if (b->inflight) return bfail(b, RBTP_ERR_STATE, "a batch launch is in flight");
     if (!h->initialised) return bfail(b, RBTP_ERR_STATE, "member not initialised");
     if (h->batch) return bfail(b, RBTP_ERR_STATE, "handle already belongs to a batch");
     if (h->mode != b->mode) return bfail(b, RBTP_ERR_CONFIG, "storage mode differs from the batch's");
@@ -290,10 +313,12 @@ int rbtp_batch_remove(rbtp_batch *b, rbtp_handle *h)
     if (!b || !h) return RBTP_ERR_ARG;
     auto it = std::find(b->members.begin(), b->members.end(), h);
     if (it == b->members.end()) return bfail(b, RBTP_ERR_ARG, "handle is not a member");
+    if (b->inflight) rbtp_batch_wait(b);   // a member leaving (e.g. destroyed) ends the launch first
     cudaStreamSynchronize(b->stream);
     b->members.erase(it);
     h->batch = nullptr;
     h->sample_every = 0;
+    h->stop_at = 0;
     b->dirty = true;
     return RBTP_OK;
 }
@@ -301,13 +326,23 @@ int rbtp_batch_remove(rbtp_batch *b, rbtp_handle *h)
 int rbtp_batch_set_sampling(rbtp_batch *b, rbtp_handle *h, int every)
 {
     if (!b || !h || h->batch != b || every < 0) return RBTP_ERR_ARG;
+    if (b->inflight) return bfail(b, RBTP_ERR_STATE, "a batch launch is in flight");
     h->sample_every = every;
+    if (!h->ring) {
+        const size_t stride = 1 + (size_t)NPLANEQ * h->geo.lx;
+        BCK(cudaMalloc(reinterpret_cast<void **>(&h->ring), RING_SLOTS * stride * sizeof(double)));
+        h->ring_cap = RING_SLOTS;
+        BCK(cudaStreamSynchronize(h->stream));
+        BCK(cudaMemcpy(h->status_host, h->status, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+        h->ring_drained = h->status_host->nsamp;
+    }
     return RBTP_OK;
 }
 
 int rbtp_batch_set_launch(rbtp_batch *b, int shape, int grid)
 {
     if (!b) return RBTP_ERR_ARG;
+    if (b->inflight) return bfail(b, RBTP_ERR_STATE, "a batch launch is in flight");
     if (shape < 0) {
         b->forced = false;
         b->tuned = false;
@@ -325,10 +360,12 @@ int rbtp_batch_set_launch(rbtp_batch *b, int shape, int grid)
     return RBTP_OK;
 }
 
-int rbtp_batch_step(rbtp_batch *b, int nsteps)
+int rbtp_batch_launch(rbtp_batch *b, int nsteps)
 {
     if (!b || nsteps < 0) return RBTP_ERR_ARG;
+    if (b->inflight) return bfail(b, RBTP_ERR_STATE, "a batch launch is already in flight");
     if (b->members.empty() || nsteps == 0) return RBTP_OK;
+    if (b->members.size() > 65535) return bfail(b, RBTP_ERR_CONFIG, "more than 65535 members");
     int st;
     if (b->dirty && (st = rebuild(b))) return st;
     if ((st = refresh(b))) return st;
@@ -359,17 +396,82 @@ int rbtp_batch_step(rbtp_batch *b, int nsteps)
             drop_graph(b);
         }
     }
+    b->inflight = true;
+    b->inflight_steps = nsteps - done;
+    b->inflight_timed = done < nsteps;
     if (done < nsteps) {
-        if (!b->graph_valid && (st = capture(b))) return st;
+        if (!b->graph_valid && (st = capture(b))) {
+            b->inflight = false;
+            return st;
+        }
         BCK(cudaEventRecord(b->e0, b->stream));
         for (int k = done; k < nsteps; ++k) BCK(cudaGraphLaunch(b->gexec, b->stream));
         BCK(cudaEventRecord(b->e1, b->stream));
+    }
+    return RBTP_OK;
+}
+
+int rbtp_batch_wait(rbtp_batch *b)
+{
+    if (!b) return RBTP_ERR_ARG;
+    if (!b->inflight) return RBTP_OK;
+    b->inflight = false;
+    if (b->inflight_timed) {
         BCK(cudaEventSynchronize(b->e1));
         float ms = 0.f;
         BCK(cudaEventElapsedTime(&ms, b->e0, b->e1));
-        b->last_ms = ms / (nsteps - done);
+        b->last_ms = ms / b->inflight_steps;
     }
     return sync_back(b);
+}
+
+int rbtp_batch_step(rbtp_batch *b, int nsteps)
+{
+    int st = rbtp_batch_launch(b, nsteps);
+    if (st) return st;
+    return rbtp_batch_wait(b);
+}
+
+int rbtp_batch_set_stop(rbtp_batch *b, rbtp_handle *h, int stop_step)
+{
+    if (!b || !h || h->batch != b) return RBTP_ERR_ARG;
+    if (b->inflight) return bfail(b, RBTP_ERR_STATE, "a batch launch is in flight");
+    h->stop_at = stop_step;
+    return RBTP_OK;
+}
+
+int rbtp_batch_samples(rbtp_batch *b, rbtp_handle *h, rbtp_nu_row *rows, int cap, int *nrows)
+{
+    if (!b || !h || h->batch != b || (!rows && cap > 0) || cap < 0) return RBTP_ERR_ARG;
+    if (b->inflight) return bfail(b, RBTP_ERR_STATE, "a batch launch is in flight");
+    if (nrows) *nrows = 0;
+    if (!h->ring) return RBTP_OK;
+    const int total = h->status_host->nsamp;   // current after the last batch step
+    int status = RBTP_OK;
+    if (total - h->ring_drained > h->ring_cap) {  // the ring wrapped: the oldest samples are gone
+        h->ring_drained = total - h->ring_cap;
+        status = RBTP_ERR_CAPACITY;
+        b->err = "sample ring overrun: samples lost (drain more often or sample less often)";
+    }
+    const int n = std::min(total - h->ring_drained, cap);
+    if (n <= 0) return status;
+    const size_t stride = 1 + (size_t)NPLANEQ * h->geo.lx;
+    std::vector<double> buf((size_t)n * stride);
+    const int s0 = h->ring_drained % h->ring_cap;
+    const int first = std::min(n, h->ring_cap - s0);
+    BCK(cudaMemcpy(buf.data(), h->ring + (size_t)s0 * stride, (size_t)first * stride * sizeof(double),
+                   cudaMemcpyDeviceToHost));
+    if (n > first)
+        BCK(cudaMemcpy(buf.data() + (size_t)first * stride, h->ring, (size_t)(n - first) * stride * sizeof(double),
+                       cudaMemcpyDeviceToHost));
+    for (int k = 0; k < n; ++k) {
+        const double *slot = buf.data() + (size_t)k * stride;
+        const int st = nu_from_planes(h, slot + 1, (int)slot[0], &rows[k]);
+        if (st && status == RBTP_OK) status = st;
+    }
+    h->ring_drained += n;
+    if (nrows) *nrows = n;
+    return status;
 }
 
 int rbtp_batch_stats_get(rbtp_batch *b, rbtp_batch_stats *o)
@@ -398,4 +500,10 @@ int rbtp_batch_stats_get(rbtp_batch *b, rbtp_batch_stats *o)
 void rbtp_batch_detach(rbtp_handle *h)
 {
     if (h && h->batch) rbtp_batch_remove(h->batch, h);
+}
+
+// A member's buffers are in use by a batch launch in flight.
+bool rbtp_batch_busy(const rbtp_handle *h)
+{
+    return h && h->batch && h->batch->inflight;
 }

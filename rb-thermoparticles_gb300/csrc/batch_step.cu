@@ -16,14 +16,22 @@ namespace {
 __device__ __forceinline__ bool hits(int istep, int every) { return every > 0 && istep % every == 0; }
 
 // Decide every cavity's output mode for the coming step (the cadence logic of main.cu:98-114 plus
-// the batch's sampling cadence) and reset the per-step particle counters.
+// the batch's sampling cadence and stop step) and reset the per-step particle counters.  A cavity
+// at its stop step is idle: every batched kernel skips it and its state stays as it is.
 __global__ void k_batch_plan(CavDesc *desc, int n)
 {
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
         CavDesc &d = desc[m];
+        if (d.stop_at > 0 && d.istep >= d.stop_at) {
+            d.out = OUT_IDLE;
+            d.samp_now = 0;
+            continue;
+        }
         const int istep = d.istep + 1;
+        const bool samp = d.samp != nullptr && (hits(istep, d.every) || istep == d.stop_at);
         const bool macro = hits(istep, d.ndiag) || hits(istep, d.nnuout) || hits(istep, d.nflowout) ||
-                           istep == d.nend || hits(istep, d.every);
+                           istep == d.nend || hits(istep, d.every) || samp;
+        d.samp_now = samp ? 1 : 0;
         d.out = macro ? OUT_MACROS : (d.pb.np > 0 ? OUT_RHO : OUT_NONE);
         if (d.pb.np > 0) {
             d.status->nf_count = 0;
@@ -36,6 +44,8 @@ __global__ void k_batch_advance(CavDesc *desc, int n)
 {
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
         CavDesc &d = desc[m];
+        if (d.out == OUT_IDLE) continue;
+        d.last_out = d.out;
         d.cur ^= 1;
         if (d.pb.np > 0) d.ocur ^= 1;
         d.phase = 1;
@@ -67,7 +77,7 @@ __global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MI
         const int4 tl = tiles[t];
         const CavDesc &d = desc[tl.x];
         const int ix = tl.y * TX + threadIdx.x, iy = tl.z * TY + threadIdx.y, iz = tl.w;
-        if (ix >= d.geo.lx || iy >= d.geo.ly) continue;
+        if (d.out == OUT_IDLE || ix >= d.geo.lx || iy >= d.geo.ly) continue;
         const int cur = d.cur;
         StepBuffers b;
         b.fin = d.f[cur];

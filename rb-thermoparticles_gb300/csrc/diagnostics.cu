@@ -20,15 +20,12 @@ namespace {
 
 constexpr int PLANE_TX = 128;
 
-__global__ void __launch_bounds__(PLANE_TX) k_plane_partial(const Geo geo, const Phys ph,
-                                                            const double *ux, const double *uy,
-                                                            const double *uz, const double *phi,
-                                                            const int *owner, const double *pst,
-                                                            int np, double *partials, int nchunks)
+// Sums of plane ix over row chunk `chunk` of nchunks (rows = (y, z) pairs in z-major order).
+__device__ __forceinline__ void plane_partial_body(const Geo &geo, const Phys &ph, const double *ux,
+                                                   const double *uy, const double *uz, const double *phi,
+                                                   const int *owner, const double *pst, int np,
+                                                   double *partials, int nchunks, int ix, int chunk)
 {
-    const int ix = blockIdx.x * PLANE_TX + threadIdx.x;
-    const int chunk = blockIdx.y;
-    if (ix >= geo.lx) return;
     const long long rows = (long long)geo.ly * geo.lz;
     const long long r0 = rows * chunk / nchunks, r1 = rows * (chunk + 1) / nchunks;
     double q[NPLANEQ];
@@ -68,14 +65,61 @@ __global__ void __launch_bounds__(PLANE_TX) k_plane_partial(const Geo geo, const
     for (int k = 0; k < NPLANEQ; ++k) partials[((long long)chunk * NPLANEQ + k) * geo.lx + ix] = q[k];
 }
 
+__global__ void __launch_bounds__(PLANE_TX) k_plane_partial(const Geo geo, const Phys ph,
+                                                            const double *ux, const double *uy,
+                                                            const double *uz, const double *phi,
+                                                            const int *owner, const double *pst,
+                                                            int np, double *partials, int nchunks)
+{
+    const int ix = blockIdx.x * PLANE_TX + threadIdx.x;
+    if (ix >= geo.lx) return;
+    plane_partial_body(geo, ph, ux, uy, uz, phi, owner, pst, np, partials, nchunks, ix, blockIdx.y);
+}
+
+// Chunks are combined in ascending order: the plane sums are deterministic and identical in the
+// single-cavity and the batched reductions.
+__device__ __forceinline__ double plane_final_body(const double *partials, int nchunks, int lx, int t)
+{
+    const int k = t / lx, ix = t - k * lx;
+    double s = 0.0;
+    for (int c = 0; c < nchunks; ++c) s += partials[((long long)c * NPLANEQ + k) * lx + ix];
+    return s;
+}
+
 __global__ void k_plane_final(const Geo geo, const double *partials, int nchunks, double *plane)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= NPLANEQ * geo.lx) return;
-    const int k = t / geo.lx, ix = t - k * geo.lx;
-    double s = 0.0;
-    for (int c = 0; c < nchunks; ++c) s += partials[((long long)c * NPLANEQ + k) * geo.lx + ix];
-    plane[t] = s;
+    plane[t] = plane_final_body(partials, nchunks, geo.lx, t);
+}
+
+// Batched sampling, after the step's advance: cavities with samp_now set reduce their current
+// macroscopic fields (owners of the new solid flags, particle state after the update) exactly as
+// the single-cavity reduction does, and the final pass writes (step, plane sums) into the next slot
+// of the cavity's sample ring and bumps its sample counter.
+__global__ void __launch_bounds__(PLANE_TX) k_batch_sample_partial(const CavDesc *desc)
+{
+    const CavDesc &d = desc[blockIdx.y];
+    if (!d.samp_now) return;
+    const int *owner = d.pb.np > 0 ? d.owner[d.ocur] : nullptr;
+    for (int chunk = blockIdx.x; chunk < d.nchunks; chunk += gridDim.x)
+        for (int ix = threadIdx.x; ix < d.geo.lx; ix += PLANE_TX)
+            plane_partial_body(d.geo, d.ph, d.ux, d.uy, d.uz, d.phi, owner, d.pb.state, d.pb.np, d.partials,
+                               d.nchunks, ix, chunk);
+}
+
+__global__ void k_batch_sample_final(const CavDesc *desc)
+{
+    const CavDesc &d = desc[blockIdx.x];
+    if (!d.samp_now) return;
+    const int lx = d.geo.lx;
+    const int slot = d.status->nsamp % d.samp_cap;
+    double *dst = d.samp + (long long)slot * (1 + NPLANEQ * lx);
+    for (int t = threadIdx.x; t < NPLANEQ * lx; t += blockDim.x)
+        dst[1 + t] = plane_final_body(d.partials, d.nchunks, lx, t);
+    if (threadIdx.x == 0) dst[0] = (double)d.istep;
+    __syncthreads();
+    if (threadIdx.x == 0) d.status->nsamp += 1;
 }
 
 // compute_Ked (collision.cu:91-152) and compute_ted (collision.cu:154-198) on the FP64 copy of
@@ -133,6 +177,14 @@ __global__ void k_dissipation(const Geo geo, const Phys ph, const double *fcol, 
 }
 
 }  // namespace
+
+cudaError_t launch_batch_sample(const CavDesc *desc, int n, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_batch_sample_partial<<<dim3(64, n), PLANE_TX, 0, st>>>(desc);
+    k_batch_sample_final<<<n, 256, 0, st>>>(desc);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_plane_sums(const Geo &geo, const Phys &ph, const double *ux, const double *uy,
                               const double *uz, const double *phi, const int *owner,

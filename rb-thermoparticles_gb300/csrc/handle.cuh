@@ -18,6 +18,10 @@ struct rbtp_handle {
     // batch membership (batch.cu)
     struct rbtp_batch *batch = nullptr;
     int sample_every = 0;
+    int stop_at = 0;                 // batched runs: step at which the cavity stops (<= 0: never)
+    double *ring = nullptr;          // batched runs: device sample ring (step + plane sums per slot)
+    int ring_cap = 0;
+    int ring_drained = 0;            // samples already turned into Nu rows
     rbtp_config cfg;
     rbtp_derived der;
     Geo geo;
@@ -50,4 +54,11 @@ struct rbtp_handle {
     bool dissip_valid = false;
     std::string err;
 };
+
+bool rbtp_batch_busy(const rbtp_handle *h);  // batch.cu
+
+namespace rbtp {
+// The Nu row of output_nu (output_statis.cu:111-223) from the ten plane sums of a state.
+int nu_from_planes(rbtp_handle *h, const double *planes, int istep, rbtp_nu_row *row);
+}  // namespace rbtp
 

@@ -134,7 +134,7 @@ constexpr int IBB_THREADS = 128;
 template <int MODE>
 __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
                                                const int *owner_cur, void *f_, void *g_,
-                                               const double *rho, int p, double *sh)
+                                               const double *rho, int p, int chunk, double *sh)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
@@ -157,7 +157,7 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
     const float mom_k = (float)(2.0 * ph.rho0 * 3.0);   // 2 rho0 / c_s^2 (float modes)
     const RR Tpr = (RR)Tp;
 
-    for (int t = threadIdx.x; t < n; t += IBB_THREADS) {
+    for (int t = chunk * IBB_THREADS + threadIdx.x; t < n; t += IBB_CHUNKS * IBB_THREADS) {
         const int x = pb.link_node[base + t];
         const int ip = pb.link_dir[base + t];
         const RR q = (RR)pb.link_q[base + t];
@@ -245,19 +245,19 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
     }
     block_reduce_fixed<7, IBB_THREADS>(acc, sh);
     if (threadIdx.x == 0) {
-        pb.hF[p] = acc[0]; pb.hF[np + p] = acc[1]; pb.hF[2 * np + p] = acc[2];
-        pb.hT[p] = acc[3]; pb.hT[np + p] = acc[4]; pb.hT[2 * np + p] = acc[5];
-        pb.hQ[p] = acc[6];
+        double *out = pb.hpart + ((long long)p * IBB_CHUNKS + chunk) * 7;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) out[q] = acc[q];
     }
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(IBB_THREADS) k_links_ibb(const Geo geo, const Phys ph,
+__global__ void __launch_bounds__(IBB_THREADS, MODE == RBTP_STORE_F64 ? 4 : 6) k_links_ibb(const Geo geo, const Phys ph,
                                                            const PartBuffers pb, void *f_,
                                                            void *g_, const double *rho)
 {
     __shared__ double sh[7 * IBB_THREADS];
-    links_ibb_body<MODE>(geo, ph, pb, pb.owner_cur, f_, g_, rho, blockIdx.x, sh);
+    links_ibb_body<MODE>(geo, ph, pb, pb.owner_cur, f_, g_, rho, blockIdx.x, blockIdx.y, sh);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -334,46 +334,59 @@ __global__ void k_cell_fill(const PartBuffers pb)
 }
 
 constexpr int MAX_CAND = 64;
+constexpr int BOX_THREADS = 512;   // CTA size of the per-particle box scans (marking, new fluid)
 
+constexpr int CONTACT_WARPS = 4;   // particles per 128-thread CTA, one warp each
+
+// One warp per particle: lane k < 27 scans neighbour cell k of the particle's cell, accepted
+// partners are collected in shared memory, and lane 0 sorts them and adds the pair forces in
+// ascending partner order (the order pforces.cu's pair loop adds them to p), then the walls.
 __device__ __forceinline__ void contact_force_body(const Geo &geo, const Phys &ph,
-                                                   const PartBuffers &pb, DevStatus *status, int p)
+                                                   const PartBuffers &pb, DevStatus *status, int p,
+                                                   int *cand /* MAX_CAND */, int &ncand)
 {
+    const int lane = threadIdx.x & 31;
     const int np = pb.np;
     const double *st = pb.state;
     const double x = PCOL(st, np, 0, p), y = PCOL(st, np, 1, p), z = PCOL(st, np, 2, p);
     const double radius = ph.radius, coeff = ph.rep_coeff, min_gap = ph.min_gap;
-    int cand[MAX_CAND];
-    int nc = 0;
-    if (np > 1) {
+    if (lane == 0) ncand = 0;
+    __syncwarp();
+    if (np > 1 && lane < 27) {
         const int cx = cell_of(x, pb.cell_size, pb.ncell[0]);
         const int cy = cell_of(y, pb.cell_size, pb.ncell[1]);
         const int cz = cell_of(z, pb.cell_size, pb.ncell[2]);
-        for (int kz = max(cz - 1, 0); kz <= min(cz + 1, pb.ncell[2] - 1); ++kz)
-            for (int ky = max(cy - 1, 0); ky <= min(cy + 1, pb.ncell[1] - 1); ++ky)
-                for (int kx = max(cx - 1, 0); kx <= min(cx + 1, pb.ncell[0] - 1); ++kx) {
-                    const int c = (kz * pb.ncell[1] + ky) * pb.ncell[0] + kx;
-                    const int s0 = pb.cell_start[c], s1 = s0 + pb.cell_count[c];
-                    for (int s = s0; s < s1; ++s) {
-                        const int q = pb.cell_items[s];
-                        if (q == p) continue;
-                        const double dx = dsub(x, PCOL(st, np, 0, q));
-                        const double dy = dsub(y, PCOL(st, np, 1, q));
-                        const double dz = dsub(z, PCOL(st, np, 2, q));
-                        const double dsq = sq3(dx, dy, dz);
-                        if (dsq <= 1.0e-12) continue;
-                        const double hgap = dsub(__dsqrt_rn(dsq), dmul(2.0, radius));
-                        if (hgap >= min_gap) continue;
-                        if (nc < MAX_CAND) cand[nc++] = q;
-                        else atomicOr(&status->contact_overflow, 1);
-                    }
-                }
-        // ascending partner order = the order pforces.cu's pair loop adds them to p
-        for (int i = 1; i < nc; ++i) {
-            const int v = cand[i];
-            int j = i - 1;
-            while (j >= 0 && cand[j] > v) { cand[j + 1] = cand[j]; --j; }
-            cand[j + 1] = v;
+        const int kx = cx + lane % 3 - 1, ky = cy + (lane / 3) % 3 - 1, kz = cz + lane / 9 - 1;
+        if (kx >= 0 && kx < pb.ncell[0] && ky >= 0 && ky < pb.ncell[1] && kz >= 0 && kz < pb.ncell[2]) {
+            const int c = (kz * pb.ncell[1] + ky) * pb.ncell[0] + kx;
+            const int s0 = pb.cell_start[c], s1 = s0 + pb.cell_count[c];
+            for (int s = s0; s < s1; ++s) {
+                const int q = pb.cell_items[s];
+                if (q == p) continue;
+                const double dx = dsub(x, PCOL(st, np, 0, q));
+                const double dy = dsub(y, PCOL(st, np, 1, q));
+                const double dz = dsub(z, PCOL(st, np, 2, q));
+                const double dsq = sq3(dx, dy, dz);
+                if (dsq <= 1.0e-12) continue;
+                const double hgap = dsub(__dsqrt_rn(dsq), dmul(2.0, radius));
+                if (hgap >= min_gap) continue;
+                const int slot = atomicAdd(&ncand, 1);
+                if (slot < MAX_CAND) cand[slot] = q;
+            }
         }
+    }
+    __syncwarp();
+    if (lane != 0) return;
+    int nc = ncand;
+    if (nc > MAX_CAND) {
+        atomicOr(&status->contact_overflow, 1);
+        nc = MAX_CAND;
+    }
+    for (int i = 1; i < nc; ++i) {
+        const int v = cand[i];
+        int j = i - 1;
+        while (j >= 0 && cand[j] > v) { cand[j + 1] = cand[j]; --j; }
+        cand[j + 1] = v;
     }
     double fx = 0.0, fy = 0.0, fz = 0.0;
     for (int i = 0; i < nc; ++i) {
@@ -420,11 +433,14 @@ __device__ __forceinline__ void contact_force_body(const Geo &geo, const Phys &p
     pb.cF[2 * np + p] = dadd(fz, wfz);
 }
 
-__global__ void k_contact_force(const Geo geo, const Phys ph, const PartBuffers pb,
-                                DevStatus *status)
+__global__ void __launch_bounds__(32 * CONTACT_WARPS) k_contact_force(const Geo geo, const Phys ph,
+                                                                     const PartBuffers pb, DevStatus *status)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < pb.np) contact_force_body(geo, ph, pb, status, p);
+    __shared__ int cand[CONTACT_WARPS][MAX_CAND];
+    __shared__ int ncand[CONTACT_WARPS];
+    const int w = threadIdx.x >> 5;
+    const int p = blockIdx.x * CONTACT_WARPS + w;
+    if (p < pb.np) contact_force_body(geo, ph, pb, status, p, cand[w], ncand[w]);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -436,40 +452,57 @@ __device__ __forceinline__ void update_body(const Phys &ph, const PartBuffers &p
     double *st = pb.state;
     const double dt = 1.0;
     const double buoyancy = (1.0 - 1.0 / ph.rho_ratio) * ph.grav0;
+    // this step's hydrodynamic force, torque and heat: the link-chunk partial sums in chunk order
+    double h[7] = {0, 0, 0, 0, 0, 0, 0};
+    const double *part = pb.hpart + (long long)p * IBB_CHUNKS * 7;
+#pragma unroll
+    for (int c = 0; c < IBB_CHUNKS; ++c)
+#pragma unroll
+        for (int q = 0; q < 7; ++q) h[q] += part[c * 7 + q];
+    // every column is read before any is written (the loads need not wait on the stores)
+    double col[33];
+#pragma unroll
+    for (int c = 0; c < 33; ++c) col[c] = PCOL(st, np, c, p);
+    double cf[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) cf[a] = pb.cF[a * np + p];
+    double out[33];
+#pragma unroll
+    for (int c = 0; c < 33; ++c) out[c] = col[c];
     double vn[3], on[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         // force / torque histories: prev2 <- prev, prev <- accum, accum <- this step's sums
-        const double f_prev = PCOL(st, np, 6 + a, p);
-        const double f_prev2 = PCOL(st, np, 9 + a, p);
-        const double t_prev = PCOL(st, np, 21 + a, p);
-        const double t_prev2 = PCOL(st, np, 24 + a, p);
-        const double f_now = pb.cF[a * np + p] + pb.hF[a * np + p];
-        const double t_now = pb.hT[a * np + p];
-        PCOL(st, np, 12 + a, p) = f_prev2;
-        PCOL(st, np, 9 + a, p) = f_prev;
-        PCOL(st, np, 6 + a, p) = f_now;
-        PCOL(st, np, 27 + a, p) = t_prev2;
-        PCOL(st, np, 24 + a, p) = t_prev;
-        PCOL(st, np, 21 + a, p) = t_now;
+        const double f_prev = col[6 + a], f_prev2 = col[9 + a];
+        const double t_prev = col[21 + a], t_prev2 = col[24 + a];
+        const double f_now = cf[a] + h[a];
+        const double t_now = h[3 + a];
+        out[12 + a] = f_prev2;
+        out[9 + a] = f_prev;
+        out[6 + a] = f_now;
+        out[27 + a] = t_prev2;
+        out[24 + a] = t_prev;
+        out[21 + a] = t_now;
         const double combo_f = 0.5 * f_now + f_prev + 0.5 * f_prev2;
         const double combo_t = 0.5 * t_now + t_prev + 0.5 * t_prev2;
-        vn[a] = PCOL(st, np, 3 + a, p) + 0.5 * dt * combo_f / ph.mass;
+        vn[a] = col[3 + a] + 0.5 * dt * combo_f / ph.mass;
         if (a == 0) vn[a] += dt * buoyancy;
-        on[a] = PCOL(st, np, 18 + a, p) + 0.5 * dt * combo_t / ph.inertia;
+        on[a] = col[18 + a] + 0.5 * dt * combo_t / ph.inertia;
     }
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        PCOL(st, np, a, p) = PCOL(st, np, a, p) + 0.5 * dt * (vn[a] + PCOL(st, np, 3 + a, p));
-        PCOL(st, np, 15 + a, p) = PCOL(st, np, 15 + a, p) + 0.5 * dt * (on[a] + PCOL(st, np, 18 + a, p));
-        PCOL(st, np, 3 + a, p) = vn[a];
-        PCOL(st, np, 18 + a, p) = on[a];
+        out[a] = col[a] + 0.5 * dt * (vn[a] + col[3 + a]);
+        out[15 + a] = col[15 + a] + 0.5 * dt * (on[a] + col[18 + a]);
+        out[3 + a] = vn[a];
+        out[18 + a] = on[a];
     }
-    const double heat_prev = PCOL(st, np, 31, p);
-    const double heat = pb.hQ[p];
-    PCOL(st, np, 32, p) = heat_prev;
-    PCOL(st, np, 31, p) = heat;
-    PCOL(st, np, 30, p) = PCOL(st, np, 30, p) + 0.5 * dt * (heat + heat_prev) / ph.heat_cap;
+    const double heat_prev = col[31];
+    const double heat = h[6];
+    out[32] = heat_prev;
+    out[31] = heat;
+    out[30] = col[30] + 0.5 * dt * (heat + heat_prev) / ph.heat_cap;
+#pragma unroll
+    for (int c = 0; c < 33; ++c) PCOL(st, np, c, p) = out[c];
 }
 
 __global__ void k_update(const Phys ph, const PartBuffers pb)
@@ -526,13 +559,18 @@ __global__ void k_mark(const Geo geo, const Phys ph, const PartBuffers pb, int *
 // ------------------------------------------------------------------------------------------------
 // Link slabs (links.cu:50-139): CTA per particle, ordered compaction over its padded box.
 // Phase 1 (integer work only): every fluid node of the box within r + 2 of the centre marks the
-// directions whose neighbour this particle owns; the candidates (node, direction) are compacted in
-// node-then-direction order into shared memory.  Phase 2: the FP64 ray-sphere q of links.cu:7-23
-// runs over the compacted candidates with all lanes busy, and accepted links are appended to the
-// particle's slab in the same order.
+// directions whose neighbour this particle owns (a 27-bit mask per node); an exclusive scan of the
+// mask popcounts numbers the candidates (node, direction) in node-then-direction order.  Phase 2:
+// candidate k is located by a binary search over the scan and a bit select in its node's mask, the
+// ray-sphere q of links.cu:7-23 runs with all lanes busy, and accepted links are appended to the
+// particle's slab in the same order.  Only the spherical shell that can hold link nodes is
+// enumerated: per (y, z) row of the box, the x-intervals between an inner radius (nodes inside it
+// are certainly solid) and the outer reach r + 2, with float margins so that every possible link
+// node is kept; rows are numbered by a block scan and flat indices are mapped back by a binary
+// search, so nodes are still visited in ascending index order (the link order is unchanged).
 // ------------------------------------------------------------------------------------------------
-constexpr int LINK_THREADS = 256;
-constexpr int LINK_CAND = LINK_THREADS * 26;
+constexpr int LINK_THREADS = 512;
+constexpr int LINK_MAX_ROWS = 2048;   // (y, z) rows of the shell table; larger boxes scan the box
 
 __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total)
 {
@@ -557,10 +595,21 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total
     return wbase + incl - v;
 }
 
+// Shared scratch of one link-fill CTA.
+struct LinkShared {
+    int wsum[LINK_THREADS / 32];
+    unsigned mask[LINK_THREADS];   // candidate directions of each chunk node (bit ip)
+    int scan[LINK_THREADS];        // exclusive prefix of the popcounts
+    int node[LINK_THREADS];        // lattice index of each chunk node
+    int row_start[LINK_MAX_ROWS];  // shell table: first flat index of each (y, z) row
+    int row_xa[LINK_MAX_ROWS];     // start and length of the row's first x-interval
+    int row_na[LINK_MAX_ROWS];
+    int row_xb[LINK_MAX_ROWS];     // start of its second x-interval
+};
+
 template <bool F32Q>
 __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                                               const int *owner, DevStatus *status, int p, int *wsum,
-                                               int *cand /* (box-local node index << 5) | direction */)
+                                               const int *owner, DevStatus *status, int p, LinkShared &sm)
 {
     const double *st = pb.state;
     const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
@@ -573,20 +622,80 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
         return;
     }
     const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
-    const int total = nx * ny * nz;
     // conservative single-precision shell test: a link needs |x - X| <= r + sqrt(3)
     const float reach = (float)r + 2.0f;
     const float reach2 = reach * reach;
     const float pxf = (float)px, pyf = (float)py, pzf = (float)pz;
+    const int rows = ny * nz;
+    const bool use_rows = rows <= LINK_MAX_ROWS;
+    int total = nx * ny * nz;
+    if (use_rows) {
+        // shell rows: |x - X| in [r_in, r_out]; nodes closer than r_in are inside the sphere
+        const float r_out = reach + 0.01f, r_in = fmaxf((float)r - 0.05f, 0.0f);
+        int carry = 0;
+        for (int r0 = 0; r0 < rows; r0 += LINK_THREADS) {
+            const int row = r0 + threadIdx.x;
+            int cnt = 0;
+            if (row < rows) {
+                const int ly = row % ny, lz = row / ny;
+                const float dy = ((float)(b.y0 + ly) + 0.5f) - pyf, dz = ((float)(b.z0 + lz) + 0.5f) - pzf;
+                const float s2 = dy * dy + dz * dz;
+                int xa = 0, na = 0, xb = 0, nb = 0;
+                if (s2 <= r_out * r_out) {
+                    const float ho = sqrtf(r_out * r_out - s2);
+                    const int xl = max(b.x0, (int)ceilf(pxf - 0.5f - ho));
+                    const int xr = min(b.x1, (int)floorf(pxf - 0.5f + ho));
+                    if (s2 < r_in * r_in) {
+                        const float hi = sqrtf(r_in * r_in - s2);
+                        const int xle = (int)floorf(pxf - 0.5f - hi), xrs = (int)ceilf(pxf - 0.5f + hi);
+                        xa = xl;
+                        na = max(0, min(xr, xle) - xl + 1);
+                        xb = max(max(xl, xrs), xle + 1);   // never re-enter the first interval
+                        nb = max(0, xr - xb + 1);
+                    } else {
+                        xa = xl;
+                        na = max(0, xr - xl + 1);
+                    }
+                }
+                cnt = na + nb;
+                sm.row_xa[row] = xa;
+                sm.row_na[row] = na;
+                sm.row_xb[row] = xb;
+            }
+            int tot;
+            const int off = block_exclusive_scan(cnt, sm.wsum, tot);
+            if (row < rows) sm.row_start[row] = carry + off;
+            carry += tot;
+        }
+        total = carry;
+        __syncthreads();
+    }
     int base = 0;
     for (int c0 = 0; c0 < total; c0 += LINK_THREADS) {
         const int t = c0 + threadIdx.x;
         unsigned mask = 0;
+        int my_node = 0;
         if (t < total) {
-            const int lz = t / (nx * ny);
-            const int rem = t - lz * nx * ny;
-            const int ly = rem / nx;
-            const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
+            int ix, iy, iz;
+            if (use_rows) {
+                int lo = 0, hi = rows - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sm.row_start[mid] <= t) lo = mid;
+                    else hi = mid - 1;
+                }
+                const int o = t - sm.row_start[lo];
+                ix = o < sm.row_na[lo] ? sm.row_xa[lo] + o : sm.row_xb[lo] + (o - sm.row_na[lo]);
+                iy = b.y0 + lo % ny;
+                iz = b.z0 + lo / ny;
+            } else {
+                const int lz = t / (nx * ny);
+                const int rem = t - lz * nx * ny;
+                const int ly = rem / nx;
+                ix = b.x0 + (rem - ly * nx);
+                iy = b.y0 + ly;
+                iz = b.z0 + lz;
+            }
             const float ddx = ((float)ix + 0.5f) - pxf, ddy = ((float)iy + 0.5f) - pyf,
                         ddz = ((float)iz + 0.5f) - pzf;
             const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
@@ -601,29 +710,34 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
                     }
                 });
             }
+            my_node = (int)idx;
         }
         int ccount;
-        int pos = block_exclusive_scan(__popc(mask), wsum, ccount);
-        while (mask) {
-            const int ip = __ffs(mask) - 1;
-            mask &= mask - 1;
-            cand[pos++] = (t << 5) | ip;
-        }
+        const int pos = block_exclusive_scan(__popc(mask), sm.wsum, ccount);
+        sm.mask[threadIdx.x] = mask;
+        sm.scan[threadIdx.x] = pos;
+        sm.node[threadIdx.x] = my_node;
         __syncthreads();
-        // phase 2: q for the compacted candidates, order-preserving append
+        // phase 2: q for the numbered candidates, order-preserving append
         for (int k0 = 0; k0 < ccount; k0 += LINK_THREADS) {
             const int k = k0 + threadIdx.x;
             int ok = 0, node = 0, ip = 0;
             double q = 0.0;
             if (k < ccount) {
-                const int cv = cand[k];
-                const int tt = cv >> 5;
-                ip = cv & 31;
-                const int lz = tt / (nx * ny);
-                const int rem = tt - lz * nx * ny;
-                const int ly = rem / nx;
-                const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
-                node = (int)((long long)iz * geo.lxy + (long long)iy * geo.lx + ix);
+                // the chunk thread j holding candidate k: the last j with scan[j] <= k
+                int lo = 0, hi = LINK_THREADS - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sm.scan[mid] <= k) lo = mid;
+                    else hi = mid - 1;
+                }
+                unsigned m = sm.mask[lo];
+                for (int r = k - sm.scan[lo]; r > 0; --r) m &= m - 1;
+                ip = __ffs(m) - 1;
+                node = sm.node[lo];
+                const int iz = node / (int)geo.lxy;
+                const int iy = (node - iz * (int)geo.lxy) / geo.lx;
+                const int ix = node - iz * (int)geo.lxy - iy * geo.lx;
                 int r32 = -1;
                 if constexpr (F32Q)
                     r32 = link_q_f32(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (float)((double)ix + 0.5 - px),
@@ -635,7 +749,7 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
                                 (double)iz + 0.5, px, py, pz, rsq, q) ? 1 : 0;
             }
             int ltotal;
-            const int lpos = base + block_exclusive_scan(ok, wsum, ltotal);
+            const int lpos = base + block_exclusive_scan(ok, sm.wsum, ltotal);
             if (ok) {
                 if (lpos < pb.link_cap) {
                     pb.link_node[slab + lpos] = node;
@@ -657,9 +771,8 @@ __global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const
                                                             const PartBuffers pb, const int *owner,
                                                             DevStatus *status)
 {
-    __shared__ int wsum[LINK_THREADS / 32];
-    __shared__ int cand[LINK_CAND];
-    link_fill_body<F32Q>(geo, ph, pb, owner, status, blockIdx.x, wsum, cand);
+    __shared__ LinkShared sm;
+    link_fill_body<F32Q>(geo, ph, pb, owner, status, blockIdx.x, sm);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -903,7 +1016,7 @@ cudaError_t launch_links_ibb(int mode, const Geo &geo, const Phys &ph, const Par
                              void *f, void *g, const double *rho, cudaStream_t st)
 {
     if (pb.np <= 0) return cudaSuccess;
-    RBTP_MODE_DISPATCH(mode, (k_links_ibb<M><<<pb.np, IBB_THREADS, 0, st>>>(geo, ph, pb, f, g, rho)));
+    RBTP_MODE_DISPATCH(mode, (k_links_ibb<M><<<dim3(pb.np, IBB_CHUNKS), IBB_THREADS, 0, st>>>(geo, ph, pb, f, g, rho)));
     return cudaGetLastError();
 }
 
@@ -920,7 +1033,7 @@ cudaError_t launch_contacts(const Geo &geo, const Phys &ph, const PartBuffers &p
     k_cell_count<<<bl, t, 0, st>>>(pb);
     k_cell_scan<<<1, 1024, 0, st>>>(pb, ncells);
     k_cell_fill<<<bl, t, 0, st>>>(pb);
-    k_contact_force<<<bl, t, 0, st>>>(geo, ph, pb, status);
+    k_contact_force<<<(pb.np + CONTACT_WARPS - 1) / CONTACT_WARPS, 32 * CONTACT_WARPS, 0, st>>>(geo, ph, pb, status);
     return cudaGetLastError();
 }
 
@@ -937,7 +1050,7 @@ cudaError_t launch_mark(const Geo &geo, const Phys &ph, const PartBuffers &pb, i
     cudaError_t e = cudaMemsetAsync(owner_out, 0xFF, sizeof(int) * (size_t)geo.L, st);
     if (e) return e;
     if (pb.np <= 0) return cudaSuccess;
-    k_mark<<<pb.np, 256, 0, st>>>(geo, ph, pb, owner_out);
+    k_mark<<<pb.np, BOX_THREADS, 0, st>>>(geo, ph, pb, owner_out);
     return cudaGetLastError();
 }
 
@@ -965,7 +1078,7 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
     if (pb.np <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(&status->nf_count, 0, sizeof(int), st);
     if (e) return e;
-    k_new_fluid<<<pb.np, 256, 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
+    k_new_fluid<<<pb.np, BOX_THREADS, 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
     RBTP_MODE_DISPATCH(mode, (k_refill_compute<M><<<152, 256, 0, st>>>(geo, ph, pb, owner_prev, f, g, status)));
     RBTP_MODE_DISPATCH(mode, (k_refill_scatter<M><<<152, 256, 0, st>>>(geo, ph, pb, f, g, faux, rho_wall, macros, rho, ux, uy, uz, phi, status)));
     return cudaGetLastError();
@@ -980,18 +1093,20 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
 namespace {
 
 template <int MODE>
-__global__ void __launch_bounds__(IBB_THREADS) k_links_ibb_b(const CavDesc *desc, const int2 *pmap)
+__global__ void __launch_bounds__(IBB_THREADS, MODE == RBTP_STORE_F64 ? 4 : 6) k_links_ibb_b(const CavDesc *desc, const int2 *pmap)
 {
     __shared__ double sh[7 * IBB_THREADS];
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
+    if (d.out == OUT_IDLE) return;
     const int w = d.cur ^ 1;
-    links_ibb_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f[w], d.g[w], d.rho, mp.y, sh);
+    links_ibb_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f[w], d.g[w], d.rho, mp.y, blockIdx.y, sh);
 }
 
 __global__ void k_cells_zero_b(const CavDesc *desc, const int *pmem)
 {
     const CavDesc &d = desc[pmem[blockIdx.y]];
+    if (d.out == OUT_IDLE) return;
     const int n = d.pb.ncell[0] * d.pb.ncell[1] * d.pb.ncell[2];
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
         d.pb.cell_count[c] = 0;
@@ -1004,6 +1119,7 @@ __global__ void k_cell_count_b(const CavDesc *desc, const int2 *pmap, int total)
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= total) return;
     const int2 mp = pmap[g];
+    if (desc[mp.x].out == OUT_IDLE) return;
     cell_count_body(desc[mp.x].pb, mp.y);
 }
 
@@ -1012,6 +1128,7 @@ __global__ void k_cell_scan_b(const CavDesc *desc, const int *pmem)
     __shared__ int sh[1024];
     __shared__ int carry;
     const CavDesc &d = desc[pmem[blockIdx.x]];
+    if (d.out == OUT_IDLE) return;
     cell_scan_body(d.pb, d.pb.ncell[0] * d.pb.ncell[1] * d.pb.ncell[2], sh, carry);
 }
 
@@ -1020,16 +1137,22 @@ __global__ void k_cell_fill_b(const CavDesc *desc, const int2 *pmap, int total)
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= total) return;
     const int2 mp = pmap[g];
+    if (desc[mp.x].out == OUT_IDLE) return;
     cell_fill_body(desc[mp.x].pb, mp.y);
 }
 
-__global__ void k_contact_force_b(const CavDesc *desc, const int2 *pmap, int total)
+__global__ void __launch_bounds__(32 * CONTACT_WARPS) k_contact_force_b(const CavDesc *desc, const int2 *pmap,
+                                                                       int total)
 {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ int cand[CONTACT_WARPS][MAX_CAND];
+    __shared__ int ncand[CONTACT_WARPS];
+    const int w = threadIdx.x >> 5;
+    const int g = blockIdx.x * CONTACT_WARPS + w;
     if (g >= total) return;
     const int2 mp = pmap[g];
     const CavDesc &d = desc[mp.x];
-    contact_force_body(d.geo, d.ph, d.pb, d.status, mp.y);
+    if (d.out == OUT_IDLE) return;
+    contact_force_body(d.geo, d.ph, d.pb, d.status, mp.y, cand[w], ncand[w]);
 }
 
 __global__ void k_update_b(const CavDesc *desc, const int2 *pmap, int total)
@@ -1038,12 +1161,14 @@ __global__ void k_update_b(const CavDesc *desc, const int2 *pmap, int total)
     if (g >= total) return;
     const int2 mp = pmap[g];
     const CavDesc &d = desc[mp.x];
+    if (d.out == OUT_IDLE) return;
     update_body(d.ph, d.pb, mp.y);
 }
 
 __global__ void k_owner_fill_b(const CavDesc *desc, const int *pmem)
 {
     const CavDesc &d = desc[pmem[blockIdx.y]];
+    if (d.out == OUT_IDLE) return;
     int *o = d.owner[d.ocur ^ 1];
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.geo.L;
          i += (long long)gridDim.x * blockDim.x)
@@ -1054,23 +1179,25 @@ __global__ void k_mark_b(const CavDesc *desc, const int2 *pmap)
 {
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
+    if (d.out == OUT_IDLE) return;
     mark_body(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], mp.y);
 }
 
 template <bool F32Q>
 __global__ void __launch_bounds__(LINK_THREADS) k_link_fill_b(const CavDesc *desc, const int2 *pmap)
 {
-    __shared__ int wsum[LINK_THREADS / 32];
-    __shared__ int cand[LINK_CAND];
+    __shared__ LinkShared sm;
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
-    link_fill_body<F32Q>(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], d.status, mp.y, wsum, cand);
+    if (d.out == OUT_IDLE) return;
+    link_fill_body<F32Q>(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], d.status, mp.y, sm);
 }
 
 __global__ void k_new_fluid_b(const CavDesc *desc, const int2 *pmap)
 {
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
+    if (d.out == OUT_IDLE) return;
     new_fluid_body(d.geo, d.ph, d.pb, d.owner[d.ocur], d.owner[d.ocur ^ 1], d.status, mp.y);
 }
 
@@ -1078,6 +1205,7 @@ template <int MODE>
 __global__ void k_refill_compute_b(const CavDesc *desc, const int *pmem)
 {
     const CavDesc &d = desc[pmem[blockIdx.y]];
+    if (d.out == OUT_IDLE) return;
     const int w = d.cur ^ 1;
     refill_compute_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f[w], d.g[w], d.status,
                               (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
@@ -1087,6 +1215,7 @@ template <int MODE>
 __global__ void k_refill_scatter_b(const CavDesc *desc, const int *pmem)
 {
     const CavDesc &d = desc[pmem[blockIdx.y]];
+    if (d.out == OUT_IDLE) return;
     const int w = d.cur ^ 1;
     refill_scatter_body<MODE>(d.geo, d.ph, d.pb, d.f[w], d.g[w], d.faux, d.rho_wall, d.out == OUT_MACROS,
                               d.rho, d.ux, d.uy, d.uz, d.phi, d.status,
@@ -1099,17 +1228,17 @@ cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int to
                                    int npmem, cudaStream_t st)
 {
     const int t = 128, bl = (total + t - 1) / t;
-    k_links_ibb_b<MODE><<<total, IBB_THREADS, 0, st>>>(desc, pmap);
+    k_links_ibb_b<MODE><<<dim3(total, IBB_CHUNKS), IBB_THREADS, 0, st>>>(desc, pmap);
     k_cells_zero_b<<<dim3(4, npmem), 256, 0, st>>>(desc, pmem);
     k_cell_count_b<<<bl, t, 0, st>>>(desc, pmap, total);
     k_cell_scan_b<<<npmem, 1024, 0, st>>>(desc, pmem);
     k_cell_fill_b<<<bl, t, 0, st>>>(desc, pmap, total);
-    k_contact_force_b<<<bl, t, 0, st>>>(desc, pmap, total);
+    k_contact_force_b<<<(total + CONTACT_WARPS - 1) / CONTACT_WARPS, 32 * CONTACT_WARPS, 0, st>>>(desc, pmap, total);
     k_update_b<<<bl, t, 0, st>>>(desc, pmap, total);
     k_owner_fill_b<<<dim3(64, npmem), 256, 0, st>>>(desc, pmem);
-    k_mark_b<<<total, 256, 0, st>>>(desc, pmap);
+    k_mark_b<<<total, BOX_THREADS, 0, st>>>(desc, pmap);
     k_link_fill_b<MODE != RBTP_STORE_F64><<<total, LINK_THREADS, 0, st>>>(desc, pmap);
-    k_new_fluid_b<<<total, 256, 0, st>>>(desc, pmap);
+    k_new_fluid_b<<<total, BOX_THREADS, 0, st>>>(desc, pmap);
     k_refill_compute_b<MODE><<<dim3(8, npmem), 256, 0, st>>>(desc, pmem);
     k_refill_scatter_b<MODE><<<dim3(8, npmem), 256, 0, st>>>(desc, pmem);
     return cudaGetLastError();

@@ -197,11 +197,13 @@ struct DevStatus {
     int contact_overflow;  // contact candidate list overflowed
     int nf_count;          // new-fluid nodes of the last refill
     int ncontacts;         // contact pairs of the last contact pass
-    int pad[2];
+    int nsamp;             // plane-sum samples written to the batch sample ring (batched runs)
+    int pad;
 };
 
 // Output selection of the step kernel.
-enum StepOut { OUT_NONE = 0, OUT_RHO = 1, OUT_MACROS = 2, OUT_MACROS_COL = 3 };
+// OUT_IDLE (batched runs only): the cavity has reached its stop step and does not advance.
+enum StepOut { OUT_NONE = 0, OUT_RHO = 1, OUT_MACROS = 2, OUT_MACROS_COL = 3, OUT_IDLE = 4 };
 
 // ------------------------------------------------------------------------------------------------
 // Kernel launch wrappers (defined in the .cu files).
@@ -235,10 +237,15 @@ cudaError_t launch_forcing(const Geo &geo, const Phys &ph, const double *phi, do
                            cudaStream_t st);
 
 // Particle pipeline ------------------------------------------------------------------------------
+// Link chunks of a particle's IBB pass: CTA c of particle p takes links c*128 + k*IBB_CHUNKS*128 + t;
+// the chunk partial sums are added in chunk order by the integrator (deterministic, and the same
+// in single-cavity and batched runs).
+constexpr int IBB_CHUNKS = 8;
+
 struct PartBuffers {
     int np;
     double *state;          // 33 columns x np, column-major (col c at state + c*np)
-    double *hF, *hT, *hQ;   // hydrodynamic force, torque (3*np each), heat (np)
+    double *hpart;          // IBB partial sums: np x IBB_CHUNKS x 7 (force, torque, heat)
     double *cF;             // contact force (3*np)
     int *owner_cur, *owner_new;   // solid owner maps (L each); -1 = fluid
     int link_cap;           // links per particle slab
@@ -292,7 +299,15 @@ struct CavDesc {
     int ndiag, nnuout, nflowout, nend;  // output cadence (<= 0: never)
     int every;                          // extra macro cadence (sampling), <= 0: never
     int out;                            // this step's output mode (written by the plan kernel)
-    int mode, pad;
+    int last_out;                       // output mode of the last step actually taken
+    int stop_at;                        // step at which the cavity stops advancing, <= 0: never
+    int samp_now;                       // this step ends with a plane-sum sample (plan kernel)
+    int mode;
+    // sample ring: samp_cap slots of (1 + NPLANEQ * lx) doubles (step, plane sums); null: none
+    double *samp;
+    int samp_cap;
+    int nchunks;                        // row chunks of the plane reduction (partials buffer)
+    double *partials;
 };
 
 constexpr int BATCH_SHAPES = 2;  // tile shapes of the batched step: 0 = 32x4, 1 = 64x2
@@ -310,6 +325,8 @@ cudaError_t launch_plane_sums(const Geo &geo, const Phys &ph, const double *ux, 
                               const double *uz, const double *phi, const int *owner,
                               const double *pstate, int np, double *partials, int nchunks,
                               double *plane, cudaStream_t st);
+// Batched sampling: plane sums of every cavity whose samp_now is set, into its sample ring.
+cudaError_t launch_batch_sample(const CavDesc *desc, int n, cudaStream_t st);
 cudaError_t launch_dissipation(const Geo &geo, const Phys &ph, const double *fcol,
                                const double *gcol, const double *rho, const double *ux,
                                const double *uy, const double *uz, const double *phi,

@@ -163,12 +163,18 @@ SIGNATURES = [
     ("rbtp_write_flow", C.c_int, [_H, C.c_char_p, C.c_int]),
     ("rbtp_write_fg", C.c_int, [_H, C.c_char_p, C.c_int]),
     ("rbtp_write_particles", C.c_int, [_H, C.c_char_p, C.c_int]),
+    ("rbtp_checkpoint_write", C.c_int, [_H, C.c_char_p]),
+    ("rbtp_checkpoint_read", C.c_int, [_H, C.c_char_p]),
     ("rbtp_batch_create", C.c_int, [C.c_int, C.POINTER(_H)]),
     ("rbtp_batch_destroy", C.c_int, [_H]),
     ("rbtp_batch_add", C.c_int, [_H, _H]),
     ("rbtp_batch_remove", C.c_int, [_H, _H]),
     ("rbtp_batch_set_sampling", C.c_int, [_H, _H, C.c_int]),
     ("rbtp_batch_step", C.c_int, [_H, C.c_int]),
+    ("rbtp_batch_set_stop", C.c_int, [_H, _H, C.c_int]),
+    ("rbtp_batch_samples", C.c_int, [_H, _H, C.POINTER(NuRow), C.c_int, C.POINTER(C.c_int)]),
+    ("rbtp_batch_launch", C.c_int, [_H, C.c_int]),
+    ("rbtp_batch_wait", C.c_int, [_H]),
     ("rbtp_batch_stats_get", C.c_int, [_H, C.POINTER(BatchStats)]),
     ("rbtp_batch_set_launch", C.c_int, [_H, C.c_int, C.c_int]),
     ("rbtp_footprint", C.c_int, [C.POINTER(Config), C.POINTER(C.c_size_t)]),
@@ -179,6 +185,8 @@ SIGNATURES = [
     ("rbtp_server_poll", C.c_int, [_H, C.c_int, _IP, _IP, C.POINTER(NuRow), C.c_int, _IP]),
     ("rbtp_server_request_times", C.c_int, [_H, C.c_int, _DP, _DP, _DP]),
     ("rbtp_server_stats", C.c_int, [_H, _DP, _DP, _DP, _DP]),
+    ("rbtp_server_checkpoint", C.c_int, [_H, C.c_char_p]),
+    ("rbtp_server_restore", C.c_int, [_H, C.c_char_p]),
     ("rbtp_plane_sums_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                           C.c_double, C.c_void_p, C.c_void_p]),
@@ -390,6 +398,13 @@ class Solver:
     def output_particles(self, istep: int, directory: Optional[str] = None) -> None:
         _check(self.lib.rbtp_write_particles(self._h, _b(directory), istep), self._h)
 
+    def checkpoint_write(self, path: str) -> None:
+        """Exact checkpoint of the whole step state (resumes bit for bit)."""
+        _check(self.lib.rbtp_checkpoint_write(self._h, _b(path)), self._h)
+
+    def checkpoint_read(self, path: str) -> None:
+        _check(self.lib.rbtp_checkpoint_read(self._h, _b(path)), self._h)
+
 
 class Batch:
     """Many cavities advanced in lockstep by one persistent launch per step (rbtp_batch_*)."""
@@ -416,6 +431,40 @@ class Batch:
         st = self.lib.rbtp_batch_step(self._b, nsteps)
         if st:
             raise RbtpError(st, "rbtp_batch_step")
+
+    def launch(self, nsteps: int = 1) -> None:
+        """Enqueue nsteps batch steps and return while they run (wait() ends them)."""
+        st = self.lib.rbtp_batch_launch(self._b, nsteps)
+        if st:
+            raise RbtpError(st, "rbtp_batch_launch")
+
+    def wait(self) -> None:
+        st = self.lib.rbtp_batch_wait(self._b)
+        if st:
+            raise RbtpError(st, "rbtp_batch_wait")
+
+    def set_sampling(self, solver: "Solver", every: int) -> None:
+        """On-device Nu sampling every `every` steps (0: only at the stop step) into a ring."""
+        _check(self.lib.rbtp_batch_set_sampling(self._b, solver.handle, every))
+
+    def set_stop(self, solver: "Solver", stop_step: int) -> None:
+        """The member stops advancing at step stop_step while the others go on."""
+        _check(self.lib.rbtp_batch_set_stop(self._b, solver.handle, stop_step))
+
+    def samples(self, solver: "Solver") -> np.ndarray:
+        """Nu rows (step, volume fraction, Nu bulk/top/bottom, bulk fluid/particle) of the samples
+        taken since the last call."""
+        out = []
+        buf = (NuRow * 64)()
+        while True:
+            n = C.c_int(0)
+            st = self.lib.rbtp_batch_samples(self._b, solver.handle, buf, 64, C.byref(n))
+            out.extend(buf[k].as_tuple() for k in range(n.value))
+            if st:
+                raise RbtpError(st, "rbtp_batch_samples")
+            if n.value < 64:
+                break
+        return np.array(out, dtype=np.float64).reshape(-1, 7)
 
     def set_launch(self, shape: int, grid: int = 0) -> None:
         _check(self.lib.rbtp_batch_set_launch(self._b, shape, grid))
@@ -481,6 +530,14 @@ class Server:
         v = [C.c_double() for _ in range(4)]
         _check(self.lib.rbtp_server_stats(self._s, *[C.byref(x) for x in v]))
         return dict(zip(["node_updates", "steps", "used_bytes", "clock"], [x.value for x in v]))
+
+    def checkpoint(self, directory: str) -> None:
+        """Between ticks: write every request's record and exact state under directory."""
+        _check(self.lib.rbtp_server_checkpoint(self._s, _b(directory)))
+
+    def restore(self, directory: str) -> None:
+        """Into a fresh server: resume the checkpointed requests."""
+        _check(self.lib.rbtp_server_restore(self._s, _b(directory)))
 
     def close(self) -> None:
         if self._s:

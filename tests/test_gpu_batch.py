@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from conftest import rel_l2
-from rbtp import Batch, Solver, STORE_F32, STORE_F64, workloads as W
+from rbtp import Batch, RbtpError, Solver, STORE_F32, STORE_F64, workloads as W
 
 pytestmark = pytest.mark.gpu
 
@@ -95,3 +95,58 @@ def test_membership_changes_and_sampling(lib_built):
         assert ss[k].istep == ref[k].istep
         assert rel_l2(ss[k].fg()[1], ref[k].fg()[1]) < 1e-6
     assert ss[1].nu(ss[1].istep)[0] == 10.0
+
+
+def test_stop_steps_and_device_sampling(lib_built):
+    """Members stop at their own steps inside one batch call and sample Nu on the device on their
+    own cadence; each member's state and Nu rows equal a solo run of exactly its steps (FP64: the
+    state to 1e-12 relative L2, the Nu rows to 1e-10 relative — the batched reduction is the solo
+    one, chunk by chunk)."""
+    cfgs = _cfgs(STORE_F64)
+    stops, every, nsteps = [7, 30, 19, 0], [5, 10, 0, 6], 30
+    alone = [_start(c, k) for k, c in enumerate(cfgs)]
+    mixed = [_start(c, k) for k, c in enumerate(cfgs)]
+    b = Batch(STORE_F64)
+    for s, st, ev in zip(mixed, stops, every):
+        b.add(s)
+        b.set_sampling(s, ev)
+        b.set_stop(s, st)
+    b.launch(nsteps)
+    with pytest.raises(RbtpError) as e:          # members are busy while the steps are in flight
+        mixed[0].fg()
+    assert e.value.status == -7
+    b.wait()
+    for k, (a, m) in enumerate(zip(alone, mixed)):
+        n = stops[k] if stops[k] > 0 else nsteps
+        assert m.istep == n
+        want = sorted({s for s in range(1, n + 1) if every[k] and s % every[k] == 0} |
+                      ({n} if stops[k] > 0 else set()))
+        rows, done = [], 0
+        for s in want:
+            a.step(s - done, macros_last=True)
+            done = s
+            rows.append(a.nu(s))
+        if done < n:
+            a.step(n - done)
+        got = b.samples(m)
+        assert got.shape == (len(want), 7)
+        np.testing.assert_allclose(got, np.array(rows), rtol=1e-10, atol=1e-12)
+        assert b.samples(m).shape == (0, 7)      # drained
+        fa, ga = a.fg()
+        fm, gm = m.fg()
+        assert rel_l2(gm, ga) < 1e-12
+        assert np.linalg.norm(fm - fa) / np.linalg.norm(ga) < 1e-12
+
+
+def test_sample_ring_overrun_is_reported(lib_built):
+    cfg = _cfgs(STORE_F32)[0]
+    s = _start(cfg, 0)
+    b = Batch(STORE_F32)
+    b.add(s)
+    b.set_sampling(s, 1)
+    b.step(70)                                   # 70 samples into a 64-slot ring
+    with pytest.raises(RbtpError) as e:
+        b.samples(s)
+    assert e.value.status == -8
+    got = b.samples(s)                           # the ring was resynchronised to the newest 64
+    assert got.shape == (0, 7)

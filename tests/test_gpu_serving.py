@@ -82,3 +82,49 @@ def test_oversized_request_fails_cleanly(lib_built):
             break
     assert srv.poll(big)["state"] == Server.FAILED and srv.poll(big)["status"] == -3
     assert srv.poll(ok)["state"] == Server.DONE
+
+
+def test_checkpoint_resume_mid_stream(lib_built, tmp_path):
+    """A server checkpointed between ticks and restored into a fresh server finishes every request
+    with the same Nu series as an uninterrupted server, bit for bit (exact state checkpoints)."""
+    reqs = [(_req(1), 260, 40), (_req(0), 150, 25), (_req(3), 330, 60), (_req(2), 90, 30)]
+    ref = Server(STORE_F32)
+    rids = [ref.submit(*r) for r in reqs]
+    _drain(ref, rids)
+    srv = Server(STORE_F32)
+    ids = [srv.submit(*r) for r in reqs]
+    for _ in range(3):
+        srv.tick(50)
+    mid = [srv.poll(i)["state"] for i in ids]
+    assert Server.ACTIVE in mid
+    srv.checkpoint(str(tmp_path))
+    srv.close()
+    again = Server(STORE_F32)
+    again.restore(str(tmp_path))
+    _drain(again, ids)
+    for a, b in zip(rids, ids):
+        pa, pb = ref.poll(a), again.poll(b)
+        assert pb["state"] == Server.DONE and pb["steps_done"] == pa["steps_done"]
+        np.testing.assert_array_equal(pb["series"], pa["series"])
+
+
+def test_handle_checkpoint_is_exact(lib_built, tmp_path):
+    from rbtp import Solver, STORE_F16S
+    for storage in (0, STORE_F32, STORE_F16S):
+        cfg = W.config("plain_fp64", lx=48, ly=48, lz=24, activate_particles=1, particle_diam_frac=8.0 / 48.0,
+                       particle_fraction=0.04, storage=storage)
+        a = Solver(cfg)
+        a.initialize()
+        a.step(13)
+        path = str(tmp_path / f"h{storage}.ckp")
+        a.checkpoint_write(path)
+        b = Solver(cfg)
+        b.checkpoint_read(path)
+        assert b.istep == 13
+        a.step(9, macros_last=True)
+        b.step(9, macros_last=True)
+        fa, ga = a.fg()
+        fb, gb = b.fg()
+        assert np.array_equal(fa, fb) and np.array_equal(ga, gb)
+        assert np.array_equal(a.particles(), b.particles()) and np.array_equal(a.flags(), b.flags())
+        assert a.nu(22) == b.nu(22)
