@@ -309,6 +309,7 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
         // links of one particle: fluid nodes within r + sqrt(3) of its centre, 26 directions each
         const long long lcap = 26 * shell_bound(r, r + std::sqrt(3.0));
         pb.link_cap = (int)std::min<long long>(lcap, 1LL << 30);
+        pb.ibb_chunks = ibb_chunks_for(pb.link_cap);
         const size_t ltot = (size_t)np * pb.link_cap;
         CKC(dalloc(&pb.link_node, ltot)); CKC(dalloc(&pb.link_dir, ltot)); CKC(dalloc(&pb.link_q, ltot));
         CKC(dalloc(&pb.link_cnt, (size_t)np));

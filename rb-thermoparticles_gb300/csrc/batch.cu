@@ -35,6 +35,8 @@ struct rbtp_batch {
     int ntiles[BATCH_SHAPES] = {0, 0};
     int2 *d_pmap = nullptr;
     int total_np = 0;
+    int2 *d_cmap = nullptr;    // (particle map entry, IBB link chunk) of every IBB CTA
+    int ncmap = 0;
     int *d_pmem = nullptr;
     int npmem = 0;
     bool dirty = true;
@@ -109,7 +111,7 @@ int rebuild(rbtp_batch *b)
         int st = upload(b, &b->d_tiles[s], t);
         if (st) return st;
     }
-    std::vector<int2> pmap;
+    std::vector<int2> pmap, cmap;
     std::vector<int> pmem;
     b->nodes = 0.0;
     for (int m = 0; m < n; ++m) {
@@ -117,12 +119,18 @@ int rebuild(rbtp_batch *b)
         b->nodes += (double)h->geo.L;
         if (h->pb.np > 0) {
             pmem.push_back(m);
-            for (int p = 0; p < h->pb.np; ++p) pmap.push_back(make_int2(m, p));
+            for (int p = 0; p < h->pb.np; ++p) {
+                for (int c = 0; c < h->pb.ibb_chunks; ++c) cmap.push_back(make_int2((int)pmap.size(), c));
+                pmap.push_back(make_int2(m, p));
+            }
         }
     }
     b->total_np = (int)pmap.size();
     b->npmem = (int)pmem.size();
     int st = upload(b, &b->d_pmap, pmap);
+    if (st) return st;
+    b->ncmap = (int)cmap.size();
+    st = upload(b, &b->d_cmap, cmap);
     if (st) return st;
     st = upload(b, &b->d_pmem, pmem);
     if (st) return st;
@@ -189,7 +197,8 @@ cudaError_t enqueue_step(rbtp_batch *b, int shape, int grid)
     if ((e = launch_batch_plan(b->d_desc, n, b->stream))) return e;
     if ((e = launch_step_batched(b->mode, shape, b->d_desc, b->d_tiles[shape], b->ntiles[shape], grid, b->stream)))
         return e;
-    if ((e = launch_particles_batched(b->mode, b->d_desc, b->d_pmap, b->total_np, b->d_pmem, b->npmem, b->stream)))
+    if ((e = launch_particles_batched(b->mode, b->d_desc, b->d_pmap, b->total_np, b->d_cmap, b->ncmap, b->d_pmem,
+                                        b->npmem, b->stream)))
         return e;
     if ((e = launch_batch_advance(b->d_desc, n, b->stream))) return e;
     return launch_batch_sample(b->d_desc, n, b->stream);
@@ -284,6 +293,7 @@ int rbtp_batch_destroy(rbtp_batch *b)
     drop_graph(b);
     for (int s = 0; s < BATCH_SHAPES; ++s) cudaFree(b->d_tiles[s]);
     cudaFree(b->d_pmap);
+    cudaFree(b->d_cmap);
     cudaFree(b->d_pmem);
     cudaFree(b->d_desc);
     if (b->h_desc) cudaFreeHost(b->h_desc);

@@ -42,6 +42,8 @@ __global__ void k_batch_plan(CavDesc *desc, int n)
 
 __global__ void k_batch_advance(CavDesc *desc, int n)
 {
+    pdl_wait();
+    pdl_trigger();
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
         CavDesc &d = desc[m];
         if (d.out == OUT_IDLE) continue;
@@ -73,6 +75,8 @@ template <int MODE, int TX, int TY>
 __global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MINB_F64 : RBTP_BATCH_MINB_LOW)
     k_step_batched(const CavDesc *__restrict__ desc, const int4 *__restrict__ tiles, int ntiles)
 {
+    pdl_wait();
+    pdl_trigger();
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 tl = tiles[t];
         const CavDesc &d = desc[tl.x];
@@ -98,9 +102,8 @@ template <int MODE>
 cudaError_t launch_mode(int shape, const CavDesc *desc, const int4 *tiles, int ntiles, int grid, cudaStream_t st)
 {
     if (ntiles <= 0) return cudaSuccess;
-    if (shape == 0) k_step_batched<MODE, 32, 4><<<grid, dim3(32, 4, 1), 0, st>>>(desc, tiles, ntiles);
-    else k_step_batched<MODE, 64, 2><<<grid, dim3(64, 2, 1), 0, st>>>(desc, tiles, ntiles);
-    return cudaGetLastError();
+    if (shape == 0) return pdl_launch(k_step_batched<MODE, 32, 4>, dim3(grid), dim3(32, 4, 1), st, desc, tiles, ntiles);
+    return pdl_launch(k_step_batched<MODE, 64, 2>, dim3(grid), dim3(64, 2, 1), st, desc, tiles, ntiles);
 }
 
 }  // namespace
@@ -113,8 +116,7 @@ cudaError_t launch_batch_plan(CavDesc *desc, int n, cudaStream_t st)
 
 cudaError_t launch_batch_advance(CavDesc *desc, int n, cudaStream_t st)
 {
-    k_batch_advance<<<(n + 127) / 128, 128, 0, st>>>(desc, n);
-    return cudaGetLastError();
+    return pdl_launch(k_batch_advance, dim3((n + 127) / 128), dim3(128), st, desc, n);
 }
 
 cudaError_t launch_step_batched(int mode, int shape, const CavDesc *desc, const int4 *tiles, int ntiles,

@@ -99,6 +99,8 @@ __global__ void k_plane_final(const Geo geo, const double *partials, int nchunks
 // of the cavity's sample ring and bumps its sample counter.
 __global__ void __launch_bounds__(PLANE_TX) k_batch_sample_partial(const CavDesc *desc)
 {
+    pdl_wait();
+    pdl_trigger();
     const CavDesc &d = desc[blockIdx.y];
     if (!d.samp_now) return;
     const int *owner = d.pb.np > 0 ? d.owner[d.ocur] : nullptr;
@@ -110,6 +112,8 @@ __global__ void __launch_bounds__(PLANE_TX) k_batch_sample_partial(const CavDesc
 
 __global__ void k_batch_sample_final(const CavDesc *desc)
 {
+    pdl_wait();
+    pdl_trigger();
     const CavDesc &d = desc[blockIdx.x];
     if (!d.samp_now) return;
     const int lx = d.geo.lx;
@@ -181,9 +185,9 @@ __global__ void k_dissipation(const Geo geo, const Phys ph, const double *fcol, 
 cudaError_t launch_batch_sample(const CavDesc *desc, int n, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
-    k_batch_sample_partial<<<dim3(64, n), PLANE_TX, 0, st>>>(desc);
-    k_batch_sample_final<<<n, 256, 0, st>>>(desc);
-    return cudaGetLastError();
+    cudaError_t e = pdl_launch(k_batch_sample_partial, dim3(64, n), dim3(PLANE_TX), st, desc);
+    if (e != cudaSuccess) return e;
+    return pdl_launch(k_batch_sample_final, dim3(n), dim3(256), st, desc);
 }
 
 cudaError_t launch_plane_sums(const Geo &geo, const Phys &ph, const double *ux, const double *uy,

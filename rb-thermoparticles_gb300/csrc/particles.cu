@@ -157,7 +157,7 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
     const float mom_k = (float)(2.0 * ph.rho0 * 3.0);   // 2 rho0 / c_s^2 (float modes)
     const RR Tpr = (RR)Tp;
 
-    for (int t = chunk * IBB_THREADS + threadIdx.x; t < n; t += IBB_CHUNKS * IBB_THREADS) {
+    for (int t = chunk * IBB_THREADS + threadIdx.x; t < n; t += pb.ibb_chunks * IBB_THREADS) {
         const int x = pb.link_node[base + t];
         const int ip = pb.link_dir[base + t];
         const RR q = (RR)pb.link_q[base + t];
@@ -334,7 +334,10 @@ __global__ void k_cell_fill(const PartBuffers pb)
 }
 
 constexpr int MAX_CAND = 64;
-constexpr int BOX_THREADS = 512;   // CTA size of the per-particle box scans (marking, new fluid)
+// Per-particle CTAs (box scans, link fill) are wide while fewer particles than this are in flight
+// (4 CTAs per SM of a 152-SM GB300) and narrow beyond; the results do not depend on the width.
+constexpr int PARTICLES_WIDE = 4 * 152;
+inline int box_threads(int particles) { return particles < PARTICLES_WIDE ? 512 : 128; }
 
 constexpr int CONTACT_WARPS = 4;   // particles per 128-thread CTA, one warp each
 
@@ -455,8 +458,7 @@ __device__ __forceinline__ void update_body(const Phys &ph, const PartBuffers &p
     // this step's hydrodynamic force, torque and heat: the link-chunk partial sums in chunk order
     double h[7] = {0, 0, 0, 0, 0, 0, 0};
     const double *part = pb.hpart + (long long)p * IBB_CHUNKS * 7;
-#pragma unroll
-    for (int c = 0; c < IBB_CHUNKS; ++c)
+    for (int c = 0; c < pb.ibb_chunks; ++c)
 #pragma unroll
         for (int q = 0; q < 7; ++q) h[q] += part[c * 7 + q];
     // every column is read before any is written (the loads need not wait on the stores)
@@ -569,9 +571,13 @@ __global__ void k_mark(const Geo geo, const Phys ph, const PartBuffers pb, int *
 // node is kept; rows are numbered by a block scan and flat indices are mapped back by a binary
 // search, so nodes are still visited in ascending index order (the link order is unchanged).
 // ------------------------------------------------------------------------------------------------
-constexpr int LINK_THREADS = 512;
-constexpr int LINK_MAX_ROWS = 2048;   // (y, z) rows of the shell table; larger boxes scan the box
+// CTA size: 512 threads when few particles are in flight (the per-particle chain is the latency),
+// 128 when many are (more particles per SM); the links are identical either way.
+constexpr int LINK_WIDE = 512, LINK_NARROW = 128;
+// (y, z) rows of the shell table (larger boxes scan the whole box)
+template <int NT> constexpr int link_max_rows() { return NT >= 512 ? 2048 : 1024; }
 
+template <int NT>
 __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -585,7 +591,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total
     __syncthreads();
     int wbase = 0, tot = 0;
 #pragma unroll
-    for (int k = 0; k < LINK_THREADS / 32; ++k) {
+    for (int k = 0; k < NT / 32; ++k) {
         const int s = wsum[k];
         if (k < warp) wbase += s;
         tot += s;
@@ -596,21 +602,24 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total
 }
 
 // Shared scratch of one link-fill CTA.
+template <int NT>
 struct LinkShared {
-    int wsum[LINK_THREADS / 32];
-    unsigned mask[LINK_THREADS];   // candidate directions of each chunk node (bit ip)
-    int scan[LINK_THREADS];        // exclusive prefix of the popcounts
-    int node[LINK_THREADS];        // lattice index of each chunk node
-    int row_start[LINK_MAX_ROWS];  // shell table: first flat index of each (y, z) row
-    int row_xa[LINK_MAX_ROWS];     // start and length of the row's first x-interval
-    int row_na[LINK_MAX_ROWS];
-    int row_xb[LINK_MAX_ROWS];     // start of its second x-interval
+    static constexpr int ROWS = link_max_rows<NT>();
+    int wsum[NT / 32];
+    unsigned mask[NT];        // candidate directions of each chunk node (bit ip)
+    int scan[NT];             // exclusive prefix of the popcounts
+    int node[NT];             // lattice index of each chunk node
+    int row_start[ROWS];      // shell table: first flat index of each (y, z) row
+    int row_xa[ROWS];         // start and length of the row's first x-interval
+    int row_na[ROWS];
+    int row_xb[ROWS];         // start of its second x-interval
 };
 
-template <bool F32Q>
+template <bool F32Q, int NT>
 __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                                               const int *owner, DevStatus *status, int p, LinkShared &sm)
+                                               const int *owner, DevStatus *status, int p, LinkShared<NT> &sm)
 {
+    constexpr int LINK_THREADS = NT;
     const double *st = pb.state;
     const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
     const double r = ph.radius;
@@ -627,7 +636,7 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
     const float reach2 = reach * reach;
     const float pxf = (float)px, pyf = (float)py, pzf = (float)pz;
     const int rows = ny * nz;
-    const bool use_rows = rows <= LINK_MAX_ROWS;
+    const bool use_rows = rows <= LinkShared<NT>::ROWS;
     int total = nx * ny * nz;
     if (use_rows) {
         // shell rows: |x - X| in [r_in, r_out]; nodes closer than r_in are inside the sphere
@@ -663,7 +672,7 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
                 sm.row_xb[row] = xb;
             }
             int tot;
-            const int off = block_exclusive_scan(cnt, sm.wsum, tot);
+            const int off = block_exclusive_scan<NT>(cnt, sm.wsum, tot);
             if (row < rows) sm.row_start[row] = carry + off;
             carry += tot;
         }
@@ -713,7 +722,7 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
             my_node = (int)idx;
         }
         int ccount;
-        const int pos = block_exclusive_scan(__popc(mask), sm.wsum, ccount);
+        const int pos = block_exclusive_scan<NT>(__popc(mask), sm.wsum, ccount);
         sm.mask[threadIdx.x] = mask;
         sm.scan[threadIdx.x] = pos;
         sm.node[threadIdx.x] = my_node;
@@ -749,7 +758,7 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
                                 (double)iz + 0.5, px, py, pz, rsq, q) ? 1 : 0;
             }
             int ltotal;
-            const int lpos = base + block_exclusive_scan(ok, sm.wsum, ltotal);
+            const int lpos = base + block_exclusive_scan<NT>(ok, sm.wsum, ltotal);
             if (ok) {
                 if (lpos < pb.link_cap) {
                     pb.link_node[slab + lpos] = node;
@@ -766,13 +775,12 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
     if (threadIdx.x == 0) pb.link_cnt[p] = base;
 }
 
-template <bool F32Q>
-__global__ void __launch_bounds__(LINK_THREADS) k_link_fill(const Geo geo, const Phys ph,
-                                                            const PartBuffers pb, const int *owner,
-                                                            DevStatus *status)
+template <bool F32Q, int NT>
+__global__ void __launch_bounds__(NT) k_link_fill(const Geo geo, const Phys ph, const PartBuffers pb,
+                                                  const int *owner, DevStatus *status)
 {
-    __shared__ LinkShared sm;
-    link_fill_body<F32Q>(geo, ph, pb, owner, status, blockIdx.x, sm);
+    __shared__ LinkShared<NT> sm;
+    link_fill_body<F32Q, NT>(geo, ph, pb, owner, status, blockIdx.x, sm);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1016,7 +1024,7 @@ cudaError_t launch_links_ibb(int mode, const Geo &geo, const Phys &ph, const Par
                              void *f, void *g, const double *rho, cudaStream_t st)
 {
     if (pb.np <= 0) return cudaSuccess;
-    RBTP_MODE_DISPATCH(mode, (k_links_ibb<M><<<dim3(pb.np, IBB_CHUNKS), IBB_THREADS, 0, st>>>(geo, ph, pb, f, g, rho)));
+    RBTP_MODE_DISPATCH(mode, (k_links_ibb<M><<<dim3(pb.np, pb.ibb_chunks), IBB_THREADS, 0, st>>>(geo, ph, pb, f, g, rho)));
     return cudaGetLastError();
 }
 
@@ -1050,7 +1058,7 @@ cudaError_t launch_mark(const Geo &geo, const Phys &ph, const PartBuffers &pb, i
     cudaError_t e = cudaMemsetAsync(owner_out, 0xFF, sizeof(int) * (size_t)geo.L, st);
     if (e) return e;
     if (pb.np <= 0) return cudaSuccess;
-    k_mark<<<pb.np, BOX_THREADS, 0, st>>>(geo, ph, pb, owner_out);
+    k_mark<<<pb.np, box_threads(pb.np), 0, st>>>(geo, ph, pb, owner_out);
     return cudaGetLastError();
 }
 
@@ -1064,8 +1072,14 @@ cudaError_t launch_link_fill(int mode, const Geo &geo, const Phys &ph, const Par
                              const int *owner, DevStatus *status, cudaStream_t st)
 {
     if (pb.np <= 0) return cudaSuccess;
-    if (mode == RBTP_STORE_F64) k_link_fill<false><<<pb.np, LINK_THREADS, 0, st>>>(geo, ph, pb, owner, status);
-    else k_link_fill<true><<<pb.np, LINK_THREADS, 0, st>>>(geo, ph, pb, owner, status);
+    const bool wide = pb.np < PARTICLES_WIDE;
+    if (mode == RBTP_STORE_F64) {
+        if (wide) k_link_fill<false, LINK_WIDE><<<pb.np, LINK_WIDE, 0, st>>>(geo, ph, pb, owner, status);
+        else k_link_fill<false, LINK_NARROW><<<pb.np, LINK_NARROW, 0, st>>>(geo, ph, pb, owner, status);
+    } else {
+        if (wide) k_link_fill<true, LINK_WIDE><<<pb.np, LINK_WIDE, 0, st>>>(geo, ph, pb, owner, status);
+        else k_link_fill<true, LINK_NARROW><<<pb.np, LINK_NARROW, 0, st>>>(geo, ph, pb, owner, status);
+    }
     return cudaGetLastError();
 }
 
@@ -1078,7 +1092,7 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
     if (pb.np <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(&status->nf_count, 0, sizeof(int), st);
     if (e) return e;
-    k_new_fluid<<<pb.np, BOX_THREADS, 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
+    k_new_fluid<<<pb.np, box_threads(pb.np), 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
     RBTP_MODE_DISPATCH(mode, (k_refill_compute<M><<<152, 256, 0, st>>>(geo, ph, pb, owner_prev, f, g, status)));
     RBTP_MODE_DISPATCH(mode, (k_refill_scatter<M><<<152, 256, 0, st>>>(geo, ph, pb, f, g, faux, rho_wall, macros, rho, ux, uy, uz, phi, status)));
     return cudaGetLastError();
@@ -1093,18 +1107,23 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
 namespace {
 
 template <int MODE>
-__global__ void __launch_bounds__(IBB_THREADS, MODE == RBTP_STORE_F64 ? 4 : 6) k_links_ibb_b(const CavDesc *desc, const int2 *pmap)
+__global__ void __launch_bounds__(IBB_THREADS, MODE == RBTP_STORE_F64 ? 4 : 6) k_links_ibb_b(const CavDesc *desc, const int2 *pmap, const int2 *cmap)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sh[7 * IBB_THREADS];
-    const int2 mp = pmap[blockIdx.x];
+    const int2 cm = cmap[blockIdx.x];   // (particle map entry, link chunk)
+    const int2 mp = pmap[cm.x];
     const CavDesc &d = desc[mp.x];
     if (d.out == OUT_IDLE) return;
     const int w = d.cur ^ 1;
-    links_ibb_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f[w], d.g[w], d.rho, mp.y, blockIdx.y, sh);
+    links_ibb_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f[w], d.g[w], d.rho, mp.y, cm.y, sh);
 }
 
 __global__ void k_cells_zero_b(const CavDesc *desc, const int *pmem)
 {
+    pdl_wait();
+    pdl_trigger();
     const CavDesc &d = desc[pmem[blockIdx.y]];
     if (d.out == OUT_IDLE) return;
     const int n = d.pb.ncell[0] * d.pb.ncell[1] * d.pb.ncell[2];
@@ -1116,6 +1135,8 @@ __global__ void k_cells_zero_b(const CavDesc *desc, const int *pmem)
 
 __global__ void k_cell_count_b(const CavDesc *desc, const int2 *pmap, int total)
 {
+    pdl_wait();
+    pdl_trigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= total) return;
     const int2 mp = pmap[g];
@@ -1125,6 +1146,8 @@ __global__ void k_cell_count_b(const CavDesc *desc, const int2 *pmap, int total)
 
 __global__ void k_cell_scan_b(const CavDesc *desc, const int *pmem)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int sh[1024];
     __shared__ int carry;
     const CavDesc &d = desc[pmem[blockIdx.x]];
@@ -1134,6 +1157,8 @@ __global__ void k_cell_scan_b(const CavDesc *desc, const int *pmem)
 
 __global__ void k_cell_fill_b(const CavDesc *desc, const int2 *pmap, int total)
 {
+    pdl_wait();
+    pdl_trigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= total) return;
     const int2 mp = pmap[g];
@@ -1144,6 +1169,8 @@ __global__ void k_cell_fill_b(const CavDesc *desc, const int2 *pmap, int total)
 __global__ void __launch_bounds__(32 * CONTACT_WARPS) k_contact_force_b(const CavDesc *desc, const int2 *pmap,
                                                                        int total)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int cand[CONTACT_WARPS][MAX_CAND];
     __shared__ int ncand[CONTACT_WARPS];
     const int w = threadIdx.x >> 5;
@@ -1157,6 +1184,8 @@ __global__ void __launch_bounds__(32 * CONTACT_WARPS) k_contact_force_b(const Ca
 
 __global__ void k_update_b(const CavDesc *desc, const int2 *pmap, int total)
 {
+    pdl_wait();
+    pdl_trigger();
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= total) return;
     const int2 mp = pmap[g];
@@ -1167,6 +1196,8 @@ __global__ void k_update_b(const CavDesc *desc, const int2 *pmap, int total)
 
 __global__ void k_owner_fill_b(const CavDesc *desc, const int *pmem)
 {
+    pdl_wait();
+    pdl_trigger();
     const CavDesc &d = desc[pmem[blockIdx.y]];
     if (d.out == OUT_IDLE) return;
     int *o = d.owner[d.ocur ^ 1];
@@ -1177,24 +1208,30 @@ __global__ void k_owner_fill_b(const CavDesc *desc, const int *pmem)
 
 __global__ void k_mark_b(const CavDesc *desc, const int2 *pmap)
 {
+    pdl_wait();
+    pdl_trigger();
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
     if (d.out == OUT_IDLE) return;
     mark_body(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], mp.y);
 }
 
-template <bool F32Q>
-__global__ void __launch_bounds__(LINK_THREADS) k_link_fill_b(const CavDesc *desc, const int2 *pmap)
+template <bool F32Q, int NT>
+__global__ void __launch_bounds__(NT) k_link_fill_b(const CavDesc *desc, const int2 *pmap)
 {
-    __shared__ LinkShared sm;
+    pdl_wait();
+    pdl_trigger();
+    __shared__ LinkShared<NT> sm;
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
     if (d.out == OUT_IDLE) return;
-    link_fill_body<F32Q>(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], d.status, mp.y, sm);
+    link_fill_body<F32Q, NT>(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], d.status, mp.y, sm);
 }
 
 __global__ void k_new_fluid_b(const CavDesc *desc, const int2 *pmap)
 {
+    pdl_wait();
+    pdl_trigger();
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
     if (d.out == OUT_IDLE) return;
@@ -1204,6 +1241,8 @@ __global__ void k_new_fluid_b(const CavDesc *desc, const int2 *pmap)
 template <int MODE>
 __global__ void k_refill_compute_b(const CavDesc *desc, const int *pmem)
 {
+    pdl_wait();
+    pdl_trigger();
     const CavDesc &d = desc[pmem[blockIdx.y]];
     if (d.out == OUT_IDLE) return;
     const int w = d.cur ^ 1;
@@ -1214,6 +1253,8 @@ __global__ void k_refill_compute_b(const CavDesc *desc, const int *pmem)
 template <int MODE>
 __global__ void k_refill_scatter_b(const CavDesc *desc, const int *pmem)
 {
+    pdl_wait();
+    pdl_trigger();
     const CavDesc &d = desc[pmem[blockIdx.y]];
     if (d.out == OUT_IDLE) return;
     const int w = d.cur ^ 1;
@@ -1224,36 +1265,46 @@ __global__ void k_refill_scatter_b(const CavDesc *desc, const int *pmem)
 }
 
 template <int MODE>
-cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int total, const int *pmem,
-                                   int npmem, cudaStream_t st)
+cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int total, const int2 *cmap,
+                                   int ncmap, const int *pmem, int npmem, cudaStream_t st)
 {
     const int t = 128, bl = (total + t - 1) / t;
-    k_links_ibb_b<MODE><<<dim3(total, IBB_CHUNKS), IBB_THREADS, 0, st>>>(desc, pmap);
-    k_cells_zero_b<<<dim3(4, npmem), 256, 0, st>>>(desc, pmem);
-    k_cell_count_b<<<bl, t, 0, st>>>(desc, pmap, total);
-    k_cell_scan_b<<<npmem, 1024, 0, st>>>(desc, pmem);
-    k_cell_fill_b<<<bl, t, 0, st>>>(desc, pmap, total);
-    k_contact_force_b<<<(total + CONTACT_WARPS - 1) / CONTACT_WARPS, 32 * CONTACT_WARPS, 0, st>>>(desc, pmap, total);
-    k_update_b<<<bl, t, 0, st>>>(desc, pmap, total);
-    k_owner_fill_b<<<dim3(64, npmem), 256, 0, st>>>(desc, pmem);
-    k_mark_b<<<total, BOX_THREADS, 0, st>>>(desc, pmap);
-    k_link_fill_b<MODE != RBTP_STORE_F64><<<total, LINK_THREADS, 0, st>>>(desc, pmap);
-    k_new_fluid_b<<<total, BOX_THREADS, 0, st>>>(desc, pmap);
-    k_refill_compute_b<MODE><<<dim3(8, npmem), 256, 0, st>>>(desc, pmem);
-    k_refill_scatter_b<MODE><<<dim3(8, npmem), 256, 0, st>>>(desc, pmem);
+    cudaError_t e;
+#define RBTP_PDL(...)                                                       \
+    do {                                                                    \
+        if ((e = pdl_launch(__VA_ARGS__)) != cudaSuccess) return e;         \
+    } while (0)
+    RBTP_PDL(k_links_ibb_b<MODE>, dim3(ncmap), dim3(IBB_THREADS), st, desc, pmap, cmap);
+    RBTP_PDL(k_cells_zero_b, dim3(4, npmem), dim3(256), st, desc, pmem);
+    RBTP_PDL(k_cell_count_b, dim3(bl), dim3(t), st, desc, pmap, total);
+    RBTP_PDL(k_cell_scan_b, dim3(npmem), dim3(1024), st, desc, pmem);
+    RBTP_PDL(k_cell_fill_b, dim3(bl), dim3(t), st, desc, pmap, total);
+    RBTP_PDL(k_contact_force_b, dim3((total + CONTACT_WARPS - 1) / CONTACT_WARPS), dim3(32 * CONTACT_WARPS), st,
+             desc, pmap, total);
+    RBTP_PDL(k_update_b, dim3(bl), dim3(t), st, desc, pmap, total);
+    RBTP_PDL(k_owner_fill_b, dim3(64, npmem), dim3(256), st, desc, pmem);
+    RBTP_PDL(k_mark_b, dim3(total), dim3(box_threads(total)), st, desc, pmap);
+    if (total < PARTICLES_WIDE)
+        RBTP_PDL(k_link_fill_b<MODE != RBTP_STORE_F64, LINK_WIDE>, dim3(total), dim3(LINK_WIDE), st, desc, pmap);
+    else
+        RBTP_PDL(k_link_fill_b<MODE != RBTP_STORE_F64, LINK_NARROW>, dim3(total), dim3(LINK_NARROW), st, desc, pmap);
+    RBTP_PDL(k_new_fluid_b, dim3(total), dim3(box_threads(total)), st, desc, pmap);
+    RBTP_PDL(k_refill_compute_b<MODE>, dim3(8, npmem), dim3(256), st, desc, pmem);
+    RBTP_PDL(k_refill_scatter_b<MODE>, dim3(8, npmem), dim3(256), st, desc, pmem);
+#undef RBTP_PDL
     return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_particles_batched(int mode, const CavDesc *desc, const int2 *pmap, int total_np,
-                                     const int *pmem, int npmem, cudaStream_t st)
+                                     const int2 *cmap, int ncmap, const int *pmem, int npmem, cudaStream_t st)
 {
     if (total_np <= 0 || npmem <= 0) return cudaSuccess;
     switch (mode) {
-    case RBTP_STORE_F64: return particles_batched_mode<RBTP_STORE_F64>(desc, pmap, total_np, pmem, npmem, st);
-    case RBTP_STORE_F32: return particles_batched_mode<RBTP_STORE_F32>(desc, pmap, total_np, pmem, npmem, st);
-    case RBTP_STORE_F16S: return particles_batched_mode<RBTP_STORE_F16S>(desc, pmap, total_np, pmem, npmem, st);
+    case RBTP_STORE_F64: return particles_batched_mode<RBTP_STORE_F64>(desc, pmap, total_np, cmap, ncmap, pmem, npmem, st);
+    case RBTP_STORE_F32: return particles_batched_mode<RBTP_STORE_F32>(desc, pmap, total_np, cmap, ncmap, pmem, npmem, st);
+    case RBTP_STORE_F16S: return particles_batched_mode<RBTP_STORE_F16S>(desc, pmap, total_np, cmap, ncmap, pmem, npmem, st);
     }
     return cudaErrorInvalidValue;
 }

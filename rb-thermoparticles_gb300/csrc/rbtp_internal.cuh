@@ -17,6 +17,42 @@
 
 namespace rbtp {
 
+// Programmatic dependent launch (batched step sequence).  A kernel launched by pdl_launch may be
+// scheduled while its stream predecessor is still running; it calls pdl_wait() before anything
+// else (which returns once the predecessor has completed and its writes are visible) and then
+// pdl_trigger() so that its own successor can be scheduled early.  Every such kernel waits first
+// and unconditionally, so completion of a kernel implies completion of all earlier ones.
+#ifndef RBTP_USE_PDL
+#define RBTP_USE_PDL 1
+#endif
+__device__ __forceinline__ void pdl_wait()
+{
+#if RBTP_USE_PDL
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+__device__ __forceinline__ void pdl_trigger()
+{
+#if RBTP_USE_PDL
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
+template <typename... KArgs, typename... Args>
+cudaError_t pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = RBTP_USE_PDL;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // ------------------------------------------------------------------------------------------------
 // D3Q27 tables (initial.cu:276-286)
 // ------------------------------------------------------------------------------------------------
@@ -237,15 +273,21 @@ cudaError_t launch_forcing(const Geo &geo, const Phys &ph, const double *phi, do
                            cudaStream_t st);
 
 // Particle pipeline ------------------------------------------------------------------------------
-// Link chunks of a particle's IBB pass: CTA c of particle p takes links c*128 + k*IBB_CHUNKS*128 + t;
-// the chunk partial sums are added in chunk order by the integrator (deterministic, and the same
-// in single-cavity and batched runs).
+// Link chunks of a particle's IBB pass: CTA c of particle p takes links c*128 + k*nc*128 + t, with
+// nc = PartBuffers::ibb_chunks (fixed per cavity by its sphere size, at most IBB_CHUNKS); the
+// chunk partial sums are added in chunk order by the integrator (deterministic, and the same in
+// single-cavity and batched runs).
 constexpr int IBB_CHUNKS = 8;
+constexpr int ibb_chunks_for(long long link_cap)
+{
+    return link_cap <= 2048 ? 1 : (link_cap >= 2048LL * IBB_CHUNKS ? IBB_CHUNKS : (int)((link_cap + 2047) / 2048));
+}
 
 struct PartBuffers {
     int np;
     double *state;          // 33 columns x np, column-major (col c at state + c*np)
     double *hpart;          // IBB partial sums: np x IBB_CHUNKS x 7 (force, torque, heat)
+    int ibb_chunks;         // link chunks (CTAs) per particle, 1..IBB_CHUNKS, from the link capacity
     double *cF;             // contact force (3*np)
     int *owner_cur, *owner_new;   // solid owner maps (L each); -1 = fluid
     int link_cap;           // links per particle slab
@@ -316,7 +358,7 @@ cudaError_t launch_batch_advance(CavDesc *desc, int n, cudaStream_t st);
 cudaError_t launch_step_batched(int mode, int shape, const CavDesc *desc, const int4 *tiles,
                                 int ntiles, int grid, cudaStream_t st);
 cudaError_t launch_particles_batched(int mode, const CavDesc *desc, const int2 *pmap, int total_np,
-                                     const int *pmem, int npmem, cudaStream_t st);
+                                     const int2 *cmap, int ncmap, const int *pmem, int npmem, cudaStream_t st);
 
 // Diagnostics ------------------------------------------------------------------------------------
 // Per-x-plane sums: 10 quantities x lx, see diagnostics.cu.

@@ -38,22 +38,35 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     const long long wall_slot = (long long)iz * geo.ly + iy;
     const StepK<R> &K = step_consts<R>(ph);
 
+    // Shifted-FP16 storage works in its scaled variables throughout: F_i = f_i / w_i and
+    // G_i = g_i / w_i - T0 are what the memory holds, the moments take the weights once per
+    // lattice-weight class, and the collision constants are divided by w_i (no per-population
+    // scaling on load or store).  The other modes work on f_i and g_i.
+    constexpr bool SC = MODE == RBTP_STORE_F16S;
+    auto ldf = [&](const S *p, double w) -> R {
+        if constexpr (SC) return (R)__half2float(*reinterpret_cast<const __half *>(p));
+        else return ST::ld_f(p, w, t0);
+    };
+    auto ldg = [&](const S *p, double w) -> R {
+        if constexpr (SC) return (R)__half2float(*reinterpret_cast<const __half *>(p));
+        else return ST::ld_g(p, w, t0);
+    };
     R f[27], g[27];
     unroll<27>([&](auto I) {
         constexpr int i = decltype(I)::value;
         constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i), o = dopp(i);
         constexpr double w = dweight(i);
         if constexpr (!PULL || i == 0) {
-            f[i] = ST::ld_f(fin + (long long)i * L + node, w, t0);
-            g[i] = ST::ld_g(gin + (long long)i * L + node, w, t0);
+            f[i] = ldf(fin + (long long)i * L + node, w);
+            g[i] = ldg(gin + (long long)i * L + node, w);
         } else {
             // f_i(x) = f*_i(x - c_i); a neighbour outside the box returns f*_opp(x) (bounce-back)
             const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
                              (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
             const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
             const long long src = out ? ((long long)o * L + node) : ((long long)i * L + node - off);
-            f[i] = ST::ld_f(fin + src, w, t0);
-            g[i] = ST::ld_g(gin + src, w, t0);
+            f[i] = ldf(fin + src, w);
+            g[i] = ldg(gin + src, w);
         }
     });
     if constexpr (PULL) {
@@ -69,7 +82,14 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
                 if constexpr (cx != 0) {
                     const bool ox = (cx == 1) ? xlo : xhi;
                     const bool oyz = (cy == 1 && ylo) || (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
-                    if (ox && !oyz) g[i] = wall_image(g[i], dweight(i), tw, rw);
+                    if (ox && !oyz) {
+                        if constexpr (SC) {
+                            const R wi = (R)dweight(i);
+                            g[i] = wall_image(wi * (g[i] + K.t0), dweight(i), tw, rw) * (R)(1.0 / dweight(i)) - K.t0;
+                        } else {
+                            g[i] = wall_image(g[i], dweight(i), tw, rw);
+                        }
+                    }
                 }
             });
         }
@@ -78,21 +98,53 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     // ---- moments (macrovar.cu:3-34), pairwise ----
     R rho = f[0], jx = 0, jy = 0, jz = 0;
     R phi = g[0], kx = 0, ky = 0, kz = 0;
-    unroll<13>([&](auto Kp) {
-        constexpr int i = dpair(decltype(Kp)::value);
-        constexpr int o = dopp(i);
-        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
-        const R sf = f[i] + f[o], df = f[i] - f[o];
-        const R sg = g[i] + g[o], dg = g[i] - g[o];
-        rho += sf;
-        phi += sg;
-        if constexpr (cx == 1) { jx += df; kx += dg; }
-        if constexpr (cx == -1) { jx -= df; kx -= dg; }
-        if constexpr (cy == 1) { jy += df; ky += dg; }
-        if constexpr (cy == -1) { jy -= df; ky -= dg; }
-        if constexpr (cz == 1) { jz += df; kz += dg; }
-        if constexpr (cz == -1) { jz -= df; kz -= dg; }
-    });
+    if constexpr (SC) {
+        // per weight class: sums of the scaled variables, then one multiply by the class weight
+        rho = (R)dweight(0) * f[0];
+        phi = (R)dweight(0) * g[0] + K.t0;   // sum_i w_i (G_i + T0), sum_i w_i = 1
+        unroll<3>([&](auto C) {
+            constexpr int c = decltype(C)::value + 1;
+            R r_ = 0, p_ = 0, ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+            unroll<13>([&](auto Kp) {
+                constexpr int i = dpair(decltype(Kp)::value);
+                if constexpr (dclass(i) == c) {
+                    constexpr int o = dopp(i);
+                    constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+                    const R sf = f[i] + f[o], df = f[i] - f[o];
+                    const R sg = g[i] + g[o], dg = g[i] - g[o];
+                    r_ += sf;
+                    p_ += sg;
+                    if constexpr (cx == 1) { ax += df; bx += dg; }
+                    if constexpr (cx == -1) { ax -= df; bx -= dg; }
+                    if constexpr (cy == 1) { ay += df; by += dg; }
+                    if constexpr (cy == -1) { ay -= df; by -= dg; }
+                    if constexpr (cz == 1) { az += df; bz += dg; }
+                    if constexpr (cz == -1) { az -= df; bz -= dg; }
+                }
+            });
+            constexpr R w = (R)(c == 1 ? 2.0 / 27.0 : (c == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
+            rho += w * r_;
+            phi += w * p_;
+            jx += w * ax; jy += w * ay; jz += w * az;
+            kx += w * bx; ky += w * by; kz += w * bz;
+        });
+    } else {
+        unroll<13>([&](auto Kp) {
+            constexpr int i = dpair(decltype(Kp)::value);
+            constexpr int o = dopp(i);
+            constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+            const R sf = f[i] + f[o], df = f[i] - f[o];
+            const R sg = g[i] + g[o], dg = g[i] - g[o];
+            rho += sf;
+            phi += sg;
+            if constexpr (cx == 1) { jx += df; kx += dg; }
+            if constexpr (cx == -1) { jx -= df; kx -= dg; }
+            if constexpr (cy == 1) { jy += df; ky += dg; }
+            if constexpr (cy == -1) { jy -= df; ky -= dg; }
+            if constexpr (cz == 1) { jz += df; kz += dg; }
+            if constexpr (cz == -1) { jz -= df; kz -= dg; }
+        });
+    }
     if (!(fabs(rho) < (R)1e30) || !(fabs(phi) < (R)1e30)) atomicOr(&b.status->nonfinite, 1);
 
     const R fold = (R)b.faux[node];
@@ -133,22 +185,32 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     const R pt = phi * K.tcinv;
     const R ptb = pt * ((R)1 + rho);
 
+    // scaled g: G* = g*/w - T0 = omc G + (g* - omc g)/w + (omc - 1) T0
+    const R gshift = SC ? (K.omc - (R)1) * K.t0 : (R)0;
     {
         constexpr R w0 = (R)dweight(0);
-        f[0] = K.om * f[0] + w0 * (k0 - h * k1);
-        g[0] = K.omc * g[0] + (w0 * (ptb - pt * h) - pt * rho);
+        if constexpr (SC) {
+            f[0] = K.om * f[0] + (k0 - h * k1);
+            g[0] = K.omc * g[0] + ((ptb - pt * h) - pt * rho * (R)(1.0 / dweight(0)) + gshift);
+        } else {
+            f[0] = K.om * f[0] + w0 * (k0 - h * k1);
+            g[0] = K.omc * g[0] + (w0 * (ptb - pt * h) - pt * rho);
+        }
     }
     // Pairs grouped by weight class (face, edge, corner); the class constants fold w_i into the
     // per-node coefficients and live only while their class is processed.
     unroll<3>([&](auto C) {
         constexpr int c = decltype(C)::value + 1;
-        constexpr R w = (R)(c == 1 ? 2.0 / 27.0 : (c == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
+        // class weight; 1 in the scaled variables of shifted-FP16 storage (w_i divided out)
+        constexpr R w = SC ? (R)1 : (R)(c == 1 ? 2.0 / 27.0 : (c == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
         const R wk1 = w * k1;
         const R ca = (R)4.5 * wk1, cb = w * k0 - h * wk1, c3 = (R)3 * wk1;
         const R wG = w * G;
         const R ce = (R)4.5 * wG, cd = wG - h * wG, cg = (R)3 * wG;
         const R wpt = w * pt;
-        const R ga = (R)4.5 * wpt, gb = w * ptb - h * wpt, gc = (R)3 * wpt;
+        const R ga = (R)4.5 * wpt, gc = (R)3 * wpt;
+        R gb = w * ptb - h * wpt;
+        if constexpr (SC) gb += gshift;
         const R vx = w * Vx, vy = w * Vy, vz = w * Vz;
         unroll<13>([&](auto Kp) {
             constexpr int i = dpair(decltype(Kp)::value);
@@ -180,11 +242,20 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     unroll<27>([&](auto I) {
         constexpr int i = decltype(I)::value;
         constexpr double w = dweight(i);
-        ST::st_f(fout + (long long)i * L + node, f[i], w, t0);
-        ST::st_g(gout + (long long)i * L + node, g[i], w, t0);
-        if constexpr (OUT == OUT_MACROS_COL) {
-            b.fcol[(long long)i * L + node] = (double)f[i];
-            b.gcol[(long long)i * L + node] = (double)g[i];
+        if constexpr (SC) {
+            *reinterpret_cast<__half *>(fout + (long long)i * L + node) = __float2half_rn(f[i]);
+            *reinterpret_cast<__half *>(gout + (long long)i * L + node) = __float2half_rn(g[i]);
+            if constexpr (OUT == OUT_MACROS_COL) {
+                b.fcol[(long long)i * L + node] = (double)((R)w * f[i]);
+                b.gcol[(long long)i * L + node] = (double)((R)w * (g[i] + K.t0));
+            }
+        } else {
+            ST::st_f(fout + (long long)i * L + node, f[i], w, t0);
+            ST::st_g(gout + (long long)i * L + node, g[i], w, t0);
+            if constexpr (OUT == OUT_MACROS_COL) {
+                b.fcol[(long long)i * L + node] = (double)f[i];
+                b.gcol[(long long)i * L + node] = (double)g[i];
+            }
         }
     });
 }

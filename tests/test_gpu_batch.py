@@ -4,6 +4,8 @@ alone.  Tolerances: FP64 storage 1e-12 relative L2 of the populations (the batch
 same per-node code, so agreement is normally exact); FP32 storage 1e-6.  Particle integer
 structures (solid owners) must be identical.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -150,3 +152,29 @@ def test_sample_ring_overrun_is_reported(lib_built):
     assert e.value.status == -8
     got = b.samples(s)                           # the ring was resynchronised to the newest 64
     assert got.shape == (0, 7)
+
+
+def test_particle_kernel_width_does_not_change_results(lib_built):
+    """Alone, each of three cavities has fewer than 608 spheres (wide per-particle CTAs); batched
+    together they have more (narrow CTAs).  Solid flags, link sets and states must not differ."""
+    v = 4.0 * math.pi * 2.0 ** 3 / 3.0
+    cfgs = [W.config("plain_fp64", lx=64, ly=64, lz=32, activate_particles=1, particle_diam_frac=4.0 / 64.0,
+                     particle_fraction=250.5 * v / (64 * 64 * 32), rho_particle_ratio=1.0,
+                     particle_rand_seed=100 + k, storage=STORE_F32) for k in range(3)]
+    alone = [_start(c, k) for k, c in enumerate(cfgs)]
+    mixed = [_start(c, k) for k, c in enumerate(cfgs)]
+    assert all(s.npart == 250 for s in alone)
+    b = Batch(STORE_F32)
+    for s in mixed:
+        b.add(s)
+    assert b.stats()["total_particles"] == 750
+    for s in alone:
+        s.step(12)
+    b.step(12)
+    for a, m in zip(alone, mixed):
+        assert np.array_equal(a.flags(), m.flags())
+        la, lm = a.links(), m.links()
+        for x, y in zip(la[:3], lm[:3]):
+            assert np.array_equal(x, y)
+        assert np.abs(la[3] - lm[3]).max() < 1e-5      # q from FP32 positions
+        assert rel_l2(m.fg()[1], a.fg()[1]) < 1e-6

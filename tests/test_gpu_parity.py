@@ -162,6 +162,29 @@ def test_particles_fp64_100_steps(env):
     assert np.allclose(ns, no, rtol=1e-9, atol=1e-12)
 
 
+def test_many_particles_take_the_narrow_launch_path(env):
+    """700 spheres (more than the 608 that switch the per-particle kernels to 128-thread CTAs): the
+    solid flags and link set at load are bit-exact against the oracle, and 10 FP64 steps agree."""
+    v = 4.0 * math.pi * 2.0 ** 3 / 3.0
+    cfg = _particle_cfg(lx=96, ly=96, lz=48, particle_diam_frac=4.0 / 96.0,
+                        particle_fraction=700.5 * v / (96 * 96 * 48))
+    s, o = _pair(env, cfg)
+    assert s.npart == o.npart == 700
+    s.initialize()
+    o.initialize()
+    assert np.array_equal(s.particles(), o.particles())
+    assert np.array_equal(s.flags(), o.flags())
+    _links_equal(s, o)
+    f, g, f7 = W.initial_state(cfg, seed=4)
+    p = o.particles()
+    s.load_state(f, g, f7, p)
+    o.load_state(f, g, f7, p)
+    s.step(10, macros_last=True)
+    o.step(10)
+    _compare_fields(s, o)
+    assert np.array_equal(s.flags(), o.flags())
+
+
 def test_links_contacts_new_fluid_bit_exact_at_identical_state(env):
     # hand-placed spheres: two pairs inside the contact range, one near a wall
     cfg = _particle_cfg(particle_fraction=0.01)
