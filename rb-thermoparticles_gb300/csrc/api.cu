@@ -212,6 +212,7 @@ int rbtp_footprint(const rbtp_config *cfg, size_t *bytes)
     if (np > 0) {
         const double r = d.particle_radius;
         b += (size_t)np * (NP_COLS + 7 * IBB_CHUNKS + 3) * sizeof(double);   // state, IBB partials, cF
+        b += (size_t)np * sizeof(PGeo);
         b += 2 * L * sizeof(int);                             // owner maps
         const size_t lcap = (size_t)std::min<long long>(26 * shell_bound(r, r + std::sqrt(3.0)), 1LL << 30);
         b += (size_t)np * lcap * (2 * sizeof(int) + sizeof(double)) + np * sizeof(int);
@@ -303,6 +304,7 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
         CKC(dalloc(&pb.state, (size_t)np * NP_COLS));
         CKC(cudaMemsetAsync(pb.state, 0, (size_t)np * NP_COLS * sizeof(double), h->stream));
         CKC(dalloc(&pb.hpart, (size_t)IBB_CHUNKS * 7 * np)); CKC(dalloc(&pb.cF, 3 * (size_t)np));
+        CKC(dalloc(&pb.pgeo, (size_t)np));
         CKC(dalloc(&h->owner[0], L)); CKC(dalloc(&h->owner[1], L));
         CKC(cudaMemsetAsync(h->owner[0], 0xFF, L * sizeof(int), h->stream));
         CKC(cudaMemsetAsync(h->owner[1], 0xFF, L * sizeof(int), h->stream));
@@ -352,7 +354,7 @@ int rbtp_destroy(rbtp_handle *h)
     cudaFree(h->status); if (h->status_host) cudaFreeHost(h->status_host);
     cudaFree(h->partials); cudaFree(h->plane); cudaFree(h->ring);
     PartBuffers &pb = h->pb;
-    cudaFree(pb.state); cudaFree(pb.hpart); cudaFree(pb.cF);
+    cudaFree(pb.state); cudaFree(pb.hpart); cudaFree(pb.cF); cudaFree(pb.pgeo);
     cudaFree(pb.link_node); cudaFree(pb.link_dir); cudaFree(pb.link_q); cudaFree(pb.link_cnt);
     cudaFree(pb.nf_node); cudaFree(pb.nf_pid); cudaFree(pb.nf_val); cudaFree(pb.nf_mac);
     cudaFree(pb.cell_count); cudaFree(pb.cell_start); cudaFree(pb.cell_fill); cudaFree(pb.cell_items);

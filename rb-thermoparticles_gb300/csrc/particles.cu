@@ -104,6 +104,48 @@ __device__ __forceinline__ Box sphere_box(const Geo &geo, double px, double py, 
     return b;
 }
 
+// Per-particle geometry (PGeo) of the current position; one thread per particle.
+__device__ __forceinline__ void pgeo_body(const Geo &geo, const Phys &ph, const PartBuffers &pb, int p)
+{
+    const double *st = pb.state;
+    const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
+    const double r = ph.radius;
+    PGeo g;
+    const Box m = sphere_box(geo, px, py, pz, r, 0);
+    const Box l = sphere_box(geo, px, py, pz, r, 1);
+    const Box n = sphere_box(geo, px, py, pz, dadd(r, NEW_FLUID_THRESH), 1);
+    const Box *bs[3] = {&m, &l, &n};
+    int *outs[3] = {g.mbox, g.lbox, g.nbox};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        outs[k][0] = bs[k]->x0; outs[k][1] = bs[k]->x1; outs[k][2] = bs[k]->y0;
+        outs[k][3] = bs[k]->y1; outs[k][4] = bs[k]->z0; outs[k][5] = bs[k]->z1;
+    }
+    const double c[3] = {px, py, pz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        g.ic[a] = ifloor(c[a]);
+        g.h[a] = 0.5f - (float)(c[a] - (double)g.ic[a]);
+        g.c[a] = (float)c[a];
+    }
+    // marking band: bounds the float error of |x - X|^2 (coordinate rounding ~6e-8 |X| per
+    // component, arithmetic rounding ~1e-7 relative)
+    g.rf2 = (float)dmul(r, r);
+    const float amax = fmaxf(fabsf(g.c[0]), fmaxf(fabsf(g.c[1]), fabsf(g.c[2])));
+    g.band = 1.0e-3f * g.rf2 + 1.0e-5f * (amax + 1.0f) * ((float)r + 2.0f) + 1.0e-3f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        g.v[a] = (float)PCOL(st, pb.np, 3 + a, p);
+        g.w[a] = (float)PCOL(st, pb.np, 18 + a, p);
+    }
+    g.T = (float)PCOL(st, pb.np, 30, p);
+    g.momk = (float)(2.0 * ph.rho0 * 3.0);
+    g.t0 = (float)ph.t0;
+    pb.pgeo[p] = g;
+}
+
+__device__ __forceinline__ Box pgeo_box(const int (&b)[6]) { return Box{b[0], b[1], b[2], b[3], b[4], b[5]}; }
+
 // ------------------------------------------------------------------------------------------------
 // Block reduction of NQ doubles in a fixed tree order (deterministic for a fixed block size).
 // ------------------------------------------------------------------------------------------------
@@ -124,6 +166,183 @@ __device__ __forceinline__ void block_reduce_fixed(double (&v)[NQ], double *sh /
     }
 #pragma unroll
     for (int q = 0; q < NQ; ++q) v[q] = sh[q * NT];
+}
+
+// Double-float (hi + lo, two FP32 words, ~48-bit significand) sums for the FP32/FP16 storage modes:
+// error-free TwoSum additions on the FP32 pipe instead of FP64 additions (GB300's FP64 rate is 1/64
+// of FP32).  df_add is the standard double-float addition (Knuth TwoSum of the high words, the low
+// words added into the error term, renormalised with Fast2Sum).
+struct df {
+    float hi, lo;
+};
+__device__ __forceinline__ df df_add(df a, df b)
+{
+    const float s = a.hi + b.hi;
+    const float v = s - a.hi;
+    float e = (a.hi - (s - v)) + (b.hi - v);
+    e += a.lo + b.lo;
+    const float hi = s + e;
+    return {hi, e - (hi - s)};
+}
+
+// Block reduction of NQ double-float values in a fixed order (warp shuffles, then the warps' sums
+// in warp order); the result, valid in thread 0, is returned as FP64.
+template <int NQ, int NT>
+__device__ __forceinline__ void block_reduce_df(df (&v)[NQ], double (&out)[NQ], float *sh /* 2*NQ*NT/32 */)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            const df o{__shfl_down_sync(0xffffffffu, v[q].hi, off), __shfl_down_sync(0xffffffffu, v[q].lo, off)};
+            v[q] = df_add(v[q], o);
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            sh[(2 * q) * (NT / 32) + warp] = v[q].hi;
+            sh[(2 * q + 1) * (NT / 32) + warp] = v[q].lo;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            df a{sh[(2 * q) * (NT / 32)], sh[(2 * q + 1) * (NT / 32)]};
+            for (int w = 1; w < NT / 32; ++w) a = df_add(a, df{sh[(2 * q) * (NT / 32) + w], sh[(2 * q + 1) * (NT / 32) + w]});
+            out[q] = (double)a.hi + (double)a.lo;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Block-wide exclusive scan (NT threads) and the spherical-shell row table of a particle box.
+// ------------------------------------------------------------------------------------------------
+template <int NT>
+__device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += t;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    int wbase = 0, tot = 0;
+#pragma unroll
+    for (int k = 0; k < NT / 32; ++k) {
+        const int s = wsum[k];
+        if (k < warp) wbase += s;
+        tot += s;
+    }
+    __syncthreads();
+    total = tot;
+    return wbase + incl - v;
+}
+
+// Per-particle CTAs enumerate only the nodes of a spherical shell r_in <= |x + 1/2 - X| <= r_out
+// of their box: per (y, z) row, at most two x-intervals (the caller's radii carry float margins so
+// that every node its exact test could accept is enumerated).  Rows are numbered by a block scan
+// and flat indices map back to nodes by a binary search, in ascending node index order.
+template <int NT>
+struct ShellRows {
+    static constexpr int ROWS = NT >= 512 ? 2048 : 1024;
+    int wsum[NT / 32];
+    int start[ROWS];   // first flat index of each row
+    int xa[ROWS];      // first interval: start and length
+    int na[ROWS];
+    int xb[ROWS];      // second interval: start
+};
+
+// Number of enumerated nodes, or -1 when the box has more rows than the table holds (the caller
+// then walks the whole box).  Called by all threads of the CTA; ends with a barrier.
+template <int NT>
+__device__ __forceinline__ int shell_rows_build(ShellRows<NT> &sr, const Box &b, float pxf, float pyf, float pzf,
+                                                float r_in, float r_out)
+{
+    const int ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1, rows = ny * nz;
+    if (rows > ShellRows<NT>::ROWS) return -1;
+    int carry = 0;
+    for (int r0 = 0; r0 < rows; r0 += NT) {
+        const int row = r0 + threadIdx.x;
+        int cnt = 0;
+        if (row < rows) {
+            const int ly = row % ny, lz = row / ny;
+            const float dy = ((float)(b.y0 + ly) + 0.5f) - pyf, dz = ((float)(b.z0 + lz) + 0.5f) - pzf;
+            const float s2 = dy * dy + dz * dz;
+            int xa = 0, na = 0, xb = 0, nb = 0;
+            if (s2 <= r_out * r_out) {
+                const float ho = sqrtf(r_out * r_out - s2);
+                const int xl = max(b.x0, (int)ceilf(pxf - 0.5f - ho));
+                const int xr = min(b.x1, (int)floorf(pxf - 0.5f + ho));
+                xa = xl;
+                if (s2 < r_in * r_in) {
+                    const float hi = sqrtf(r_in * r_in - s2);
+                    const int xle = (int)floorf(pxf - 0.5f - hi), xrs = (int)ceilf(pxf - 0.5f + hi);
+                    na = max(0, min(xr, xle) - xl + 1);
+                    xb = max(max(xl, xrs), xle + 1);   // never re-enter the first interval
+                    nb = max(0, xr - xb + 1);
+                } else {
+                    na = max(0, xr - xl + 1);
+                }
+            }
+            cnt = na + nb;
+            sr.xa[row] = xa;
+            sr.na[row] = na;
+            sr.xb[row] = xb;
+        }
+        int tot;
+        const int off = block_exclusive_scan<NT>(cnt, sr.wsum, tot);
+        if (row < rows) sr.start[row] = carry + off;
+        carry += tot;
+    }
+    __syncthreads();
+    return carry;
+}
+
+template <int NT>
+__device__ __forceinline__ void shell_rows_node(const ShellRows<NT> &sr, const Box &b, int t, int &ix, int &iy,
+                                                int &iz)
+{
+    const int ny = b.y1 - b.y0 + 1, rows = ny * (b.z1 - b.z0 + 1);
+    int lo = 0, hi = rows - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sr.start[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const int o = t - sr.start[lo];
+    ix = o < sr.na[lo] ? sr.xa[lo] + o : sr.xb[lo] + (o - sr.na[lo]);
+    iy = b.y0 + lo % ny;
+    iz = b.z0 + lo / ny;
+}
+
+// Calls body(ix, iy, iz) for every node of the shell (or of the whole box when the table is too
+// small), each node once, spread over the CTA.
+template <int NT, class F>
+__device__ __forceinline__ void for_shell_nodes(ShellRows<NT> &sr, const Box &b, float pxf, float pyf, float pzf,
+                                                float r_in, float r_out, F &&body)
+{
+    const int total = shell_rows_build<NT>(sr, b, pxf, pyf, pzf, r_in, r_out);
+    if (total >= 0) {
+        for (int t = threadIdx.x; t < total; t += NT) {
+            int ix, iy, iz;
+            shell_rows_node<NT>(sr, b, t, ix, iy, iz);
+            body(ix, iy, iz);
+        }
+    } else {
+        const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
+        for (int t = threadIdx.x; t < nx * ny * nz; t += NT) {
+            const int lz = t / (nx * ny);
+            const int rem = t - lz * nx * ny;
+            const int ly = rem / nx;
+            body(b.x0 + (rem - ly * nx), b.y0 + ly, b.z0 + lz);
+        }
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -150,98 +369,193 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
     const int n = min(pb.link_cnt[p], pb.link_cap);
     const long long base = (long long)p * pb.link_cap;
     double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    // Per-link arithmetic in the storage mode's arithmetic type (double for FP64 storage, float
-    // otherwise); force, torque and heat accumulate in FP64 in every mode.
-    using RR = typename ST::R;
-    const RR vxr = (RR)vx, vyr = (RR)vy, vzr = (RR)vz, wxr = (RR)wx, wyr = (RR)wy, wzr = (RR)wz;
-    const float mom_k = (float)(2.0 * ph.rho0 * 3.0);   // 2 rho0 / c_s^2 (float modes)
-    const RR Tpr = (RR)Tp;
+    if constexpr (MODE == RBTP_STORE_F64) {
+        for (int t = chunk * IBB_THREADS + threadIdx.x; t < n; t += pb.ibb_chunks * IBB_THREADS) {
+            const int x = pb.link_node[base + t];
+            const int ip = pb.link_dir[base + t];
+            const double q = pb.link_q[base + t];
+            const int iz = x / (int)geo.lxy;
+            const int rem = x - iz * (int)geo.lxy;
+            const int iy = rem / geo.lx;
+            const int ix = rem - iy * geo.lx;
+            const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
+            const int o = dopp_rt(ip);
+            const double w = dweight_rt(ip);
+            // moving wall velocity at the intersection point (ibb.cu:33-46)
+            const double relx = ((double)ix + 0.5 + q * cxi) - px;
+            const double rely = ((double)iy + 0.5 + q * cyi) - py;
+            const double relz = ((double)iz + 0.5 + q * czi) - pz;
+            const double uwx = vx + (relz * wy - rely * wz);
+            const double uwy = vy + (relx * wz - relz * wx);
+            const double uwz = vz + (rely * wx - relx * wy);
+            const double evel = (double)cxi * uwx + (double)cyi * uwy + (double)czi * uwz;
+            const double mom = 2.0 * w * ph.rho0 * evel * 3.0;
+            const double inv_2q = (q >= 0.5) ? 0.5 / q : 0.0;
 
-    for (int t = chunk * IBB_THREADS + threadIdx.x; t < n; t += pb.ibb_chunks * IBB_THREADS) {
-        const int x = pb.link_node[base + t];
-        const int ip = pb.link_dir[base + t];
-        const RR q = (RR)pb.link_q[base + t];
-        const int iz = x / (int)geo.lxy;
-        const int rem = x - iz * (int)geo.lxy;
-        const int iy = rem / geo.lx;
-        const int ix = rem - iy * geo.lx;
-        const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
-        const int o = dopp_rt(ip);
-        const double w = dweight_rt(ip);
-        const RR wr = (RR)w;
-        // moving wall velocity at the intersection point (ibb.cu:33-46); in the float modes the
-        // node-centre offset is formed in FP64 (absolute coordinates) and then rounded once
-        RR relx, rely, relz;
-        if constexpr (MODE == RBTP_STORE_F64) {
-            relx = ((double)ix + 0.5 + q * cxi) - px;
-            rely = ((double)iy + 0.5 + q * cyi) - py;
-            relz = ((double)iz + 0.5 + q * czi) - pz;
-        } else {
-            relx = (RR)((double)ix + 0.5 - px) + q * (RR)cxi;
-            rely = (RR)((double)iy + 0.5 - py) + q * (RR)cyi;
-            relz = (RR)((double)iz + 0.5 - pz) + q * (RR)czi;
-        }
-        const RR uwx = vxr + (relz * wyr - rely * wzr);
-        const RR uwy = vyr + (relx * wzr - relz * wxr);
-        const RR uwz = vzr + (rely * wxr - relx * wyr);
-        const RR evel = (RR)cxi * uwx + (RR)cyi * uwy + (RR)czi * uwz;
-        RR mom;
-        if constexpr (MODE == RBTP_STORE_F64) mom = 2.0 * w * ph.rho0 * evel * 3.0;
-        else mom = wr * mom_k * evel;
-        const RR inv_2q = (q >= (RR)0.5) ? (RR)0.5 / q : (RR)0;
+            const int ix1 = ix - cxi, iy1 = iy - cyi, iz1 = iz - czi;
+            const bool in1 = ix1 >= 0 && ix1 < geo.lx && iy1 >= 0 && iy1 < geo.ly && iz1 >= 0 && iz1 < geo.lz;
+            const long long x1 = in1 ? ((long long)iz1 * geo.lxy + (long long)iy1 * geo.lx + ix1) : 0;
+            const bool fluid1 = in1 && owner_cur[x1] < 0;
 
-        const int ix1 = ix - cxi, iy1 = iy - cyi, iz1 = iz - czi;
-        const bool in1 = ix1 >= 0 && ix1 < geo.lx && iy1 >= 0 && iy1 < geo.ly && iz1 >= 0 && iz1 < geo.lz;
-        const long long x1 = in1 ? ((long long)iz1 * geo.lxy + (long long)iy1 * geo.lx + ix1) : 0;
-        const bool fluid1 = in1 && owner_cur[x1] < 0;
-
-        const RR f_here = ST::ld_f(fB + (long long)ip * L + x, w, ph.t0);
-        const RR g_here = ST::ld_g(gB + (long long)ip * L + x, w, ph.t0);
-        const RR one = (RR)1, two = (RR)2;
-        RR fval, gval;
-        // ibb.cu:52-73 (f: q < 0.5), ibb.cu:114-128 (g: q <= 0.5)
-        if (fluid1) {
-            if (q < (RR)0.5) {
-                const RR f_up = ST::ld_f(fB + (long long)ip * L + x1, w, ph.t0);
-                fval = two * q * f_here + (one - two * q) * f_up - mom;
+            const double f_here = fB[(long long)ip * L + x];
+            const double g_here = gB[(long long)ip * L + x];
+            double fval, gval;
+            // ibb.cu:52-73 (f: q < 0.5), ibb.cu:114-128 (g: q <= 0.5)
+            if (fluid1) {
+                if (q < 0.5) {
+                    const double f_up = fB[(long long)ip * L + x1];
+                    fval = 2.0 * q * f_here + (1.0 - 2.0 * q) * f_up - mom;
+                } else {
+                    const double f_oc = fB[(long long)o * L + x];
+                    fval = (f_here - mom) * inv_2q + (2.0 * q - 1.0) * inv_2q * f_oc;
+                }
             } else {
-                const RR f_oc = ST::ld_f(fB + (long long)o * L + x, w, ph.t0);
-                fval = (f_here - mom) * inv_2q + (two * q - one) * inv_2q * f_oc;
+                fval = f_here - mom;
             }
-        } else {
-            fval = f_here - mom;
-        }
-        const RR amp = two * wr * Tpr * (RR)(1.0 + rho[x]);
-        if (fluid1) {
-            if (q <= (RR)0.5) {
-                const RR gu = ST::ld_g(gB + (long long)ip * L + x1, w, ph.t0);
-                gval = -(two * q * g_here + (one - two * q) * gu) + amp;
+            const double amp = 2.0 * w * Tp * (1.0 + rho[x]);
+            if (fluid1) {
+                if (q <= 0.5) {
+                    const double gu = gB[(long long)ip * L + x1];
+                    gval = -(2.0 * q * g_here + (1.0 - 2.0 * q) * gu) + amp;
+                } else {
+                    const double go = gB[(long long)o * L + x];
+                    gval = -g_here * inv_2q + amp * inv_2q + (2.0 * q - 1.0) * inv_2q * go;
+                }
             } else {
-                const RR go = ST::ld_g(gB + (long long)o * L + x, w, ph.t0);
-                gval = -g_here * inv_2q + amp * inv_2q + (two * q - one) * inv_2q * go;
+                gval = -g_here + amp;
             }
-        } else {
-            gval = -g_here + amp;
+            // The population that streams into x along opp comes from the solid node x + c_ip: the
+            // pull of the next step reads it from slot (opp, x + c_ip).
+            const long long solid = (long long)x + cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
+            fB[(long long)o * L + solid] = fval;
+            gB[(long long)o * L + solid] = gval;
+            // ibb.cu:160-187 (force, torque about the same intersection point) and 202-204 (heat)
+            const double Fx = (cxi - uwx) * f_here - (-cxi - uwx) * fval;
+            const double Fy = (cyi - uwy) * f_here - (-cyi - uwy) * fval;
+            const double Fz = (czi - uwz) * f_here - (-czi - uwz) * fval;
+            acc[0] += Fx;
+            acc[1] += Fy;
+            acc[2] += Fz;
+            acc[3] += rely * Fz - relz * Fy;
+            acc[4] += relz * Fx - relx * Fz;
+            acc[5] += relx * Fy - rely * Fx;
+            acc[6] += g_here - gval;
         }
-        // The population that streams into x along opp comes from the solid node x + c_ip: the
-        // pull of the next step reads it from slot (opp, x + c_ip).
-        const long long solid = (long long)x + cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
-        ST::st_f(fB + (long long)o * L + solid, fval, w, ph.t0);
-        ST::st_g(gB + (long long)o * L + solid, gval, w, ph.t0);
-        // In FP16 storage the value the reference would read back is the rounded one.
-        const RR f_out = (MODE != RBTP_STORE_F16S) ? fval : ST::ld_f(fB + (long long)o * L + solid, w, ph.t0);
-        const RR g_out = (MODE != RBTP_STORE_F16S) ? gval : ST::ld_g(gB + (long long)o * L + solid, w, ph.t0);
-        // ibb.cu:160-187 (force, torque about the same intersection point) and 202-204 (heat)
-        const RR Fx = ((RR)cxi - uwx) * f_here - ((RR)-cxi - uwx) * f_out;
-        const RR Fy = ((RR)cyi - uwy) * f_here - ((RR)-cyi - uwy) * f_out;
-        const RR Fz = ((RR)czi - uwz) * f_here - ((RR)-czi - uwz) * f_out;
-        acc[0] += (double)Fx;
-        acc[1] += (double)Fy;
-        acc[2] += (double)Fz;
-        acc[3] += (double)(rely * Fz - relz * Fy);
-        acc[4] += (double)(relz * Fx - relx * Fz);
-        acc[5] += (double)(relx * Fy - rely * Fx);
-        acc[6] += (double)(g_here - g_out);
+    } else {
+        // FP32 / shifted-FP16 storage: the per-link arithmetic runs in FP32 (GB300's FP64 rate is
+        // 1/64 of FP32).  Node-centre offsets are formed exactly from the integer part of the
+        // centre and its FP64 fraction.  Force, torque and heat are accumulated in double-float
+        // (two FP32 words, error-free additions) per thread and over the block, and leave the
+        // block as FP64 values.
+        const PGeo &pg = pb.pgeo[p];   // from the link build of these positions
+        const int ipx = pg.ic[0], ipy = pg.ic[1], ipz = pg.ic[2];
+        const float hx = pg.h[0], hy = pg.h[1], hz = pg.h[2];
+        const float vxf = pg.v[0], vyf = pg.v[1], vzf = pg.v[2];
+        const float wxf = pg.w[0], wyf = pg.w[1], wzf = pg.w[2];
+        const float mom_k = pg.momk;   // 2 rho0 / c_s^2
+        const float Tpf = pg.T, t0f = pg.t0;
+        df sum[7];
+#pragma unroll
+        for (int k = 0; k < 7; ++k) sum[k] = df{0.0f, 0.0f};
+        auto add = [&](int k, float v) { sum[k] = df_add(sum[k], df{v, 0.0f}); };
+        for (int t = chunk * IBB_THREADS + threadIdx.x; t < n; t += pb.ibb_chunks * IBB_THREADS) {
+            const int x = pb.link_node[base + t];
+            const int ip = pb.link_dir[base + t];
+            const float q = (float)pb.link_q[base + t];
+            const int iz = x / (int)geo.lxy;
+            const int rem = x - iz * (int)geo.lxy;
+            const int iy = rem / geo.lx;
+            const int ix = rem - iy * geo.lx;
+            const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
+            const int o = dopp_rt(ip);
+            const float wr = fweight_rt(ip), winv = finvweight_rt(ip);   // w_opp = w_ip
+            auto ldf = [&](const S *ptr) -> float {
+                if constexpr (MODE == RBTP_STORE_F16S) return __half2float(*ptr) * wr;
+                else return (float)*ptr;
+            };
+            auto ldg = [&](const S *ptr) -> float {
+                if constexpr (MODE == RBTP_STORE_F16S) return (__half2float(*ptr) + t0f) * wr;
+                else return (float)*ptr;
+            };
+            // moving wall velocity at the intersection point (ibb.cu:33-46)
+            const float relx = ((float)(ix - ipx) + hx) + q * (float)cxi;
+            const float rely = ((float)(iy - ipy) + hy) + q * (float)cyi;
+            const float relz = ((float)(iz - ipz) + hz) + q * (float)czi;
+            const float uwx = vxf + (relz * wyf - rely * wzf);
+            const float uwy = vyf + (relx * wzf - relz * wxf);
+            const float uwz = vzf + (rely * wxf - relx * wyf);
+            const float evel = (float)cxi * uwx + (float)cyi * uwy + (float)czi * uwz;
+            const float mom = wr * mom_k * evel;
+            const float inv_2q = (q >= 0.5f) ? 0.5f / q : 0.0f;
+
+            const int ix1 = ix - cxi, iy1 = iy - cyi, iz1 = iz - czi;
+            const bool in1 = ix1 >= 0 && ix1 < geo.lx && iy1 >= 0 && iy1 < geo.ly && iz1 >= 0 && iz1 < geo.lz;
+            const long long x1 = in1 ? ((long long)iz1 * geo.lxy + (long long)iy1 * geo.lx + ix1) : 0;
+            const bool fluid1 = in1 && owner_cur[x1] < 0;
+
+            const float f_here = ldf(fB + (long long)ip * L + x);
+            const float g_here = ldg(gB + (long long)ip * L + x);
+            float fval, gval;
+            // ibb.cu:52-73 (f: q < 0.5), ibb.cu:114-128 (g: q <= 0.5)
+            if (fluid1) {
+                if (q < 0.5f) {
+                    const float f_up = ldf(fB + (long long)ip * L + x1);
+                    fval = 2.0f * q * f_here + (1.0f - 2.0f * q) * f_up - mom;
+                } else {
+                    const float f_oc = ldf(fB + (long long)o * L + x);
+                    fval = (f_here - mom) * inv_2q + (2.0f * q - 1.0f) * inv_2q * f_oc;
+                }
+            } else {
+                fval = f_here - mom;
+            }
+            const float amp = 2.0f * wr * Tpf * (1.0f + (float)rho[x]);
+            if (fluid1) {
+                if (q <= 0.5f) {
+                    const float gu = ldg(gB + (long long)ip * L + x1);
+                    gval = -(2.0f * q * g_here + (1.0f - 2.0f * q) * gu) + amp;
+                } else {
+                    const float go = ldg(gB + (long long)o * L + x);
+                    gval = -g_here * inv_2q + amp * inv_2q + (2.0f * q - 1.0f) * inv_2q * go;
+                }
+            } else {
+                gval = -g_here + amp;
+            }
+            // The population that streams into x along opp comes from the solid node x + c_ip: the
+            // pull of the next step reads it from slot (opp, x + c_ip).
+            const long long solid = (long long)x + cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
+            S *fs = fB + (long long)o * L + solid;
+            S *gs = gB + (long long)o * L + solid;
+            float f_out = fval, g_out = gval;
+            if constexpr (MODE == RBTP_STORE_F16S) {
+                // the value the reference would read back is the rounded one
+                *fs = __float2half_rn(fval * winv);
+                *gs = __float2half_rn(gval * winv - t0f);
+                f_out = ldf(fs);
+                g_out = ldg(gs);
+            } else {
+                *fs = fval;
+                *gs = gval;
+            }
+            // ibb.cu:160-187 (force, torque about the same intersection point) and 202-204 (heat)
+            const float Fx = ((float)cxi - uwx) * f_here - ((float)-cxi - uwx) * f_out;
+            const float Fy = ((float)cyi - uwy) * f_here - ((float)-cyi - uwy) * f_out;
+            const float Fz = ((float)czi - uwz) * f_here - ((float)-czi - uwz) * f_out;
+            add(0, Fx);
+            add(1, Fy);
+            add(2, Fz);
+            add(3, rely * Fz - relz * Fy);
+            add(4, relz * Fx - relx * Fz);
+            add(5, relx * Fy - rely * Fx);
+            add(6, g_here - g_out);
+        }
+        // double-float block sum (FP32 pipe), one FP64 value per quantity
+        block_reduce_df<7, IBB_THREADS>(sum, acc, reinterpret_cast<float *>(sh));
+        if (threadIdx.x == 0) {
+            double *out = pb.hpart + ((long long)p * IBB_CHUNKS + chunk) * 7;
+#pragma unroll
+            for (int q = 0; q < 7; ++q) out[q] = acc[q];
+        }
+        return;
     }
     block_reduce_fixed<7, IBB_THREADS>(acc, sh);
     if (threadIdx.x == 0) {
@@ -334,10 +648,10 @@ __global__ void k_cell_fill(const PartBuffers pb)
 }
 
 constexpr int MAX_CAND = 64;
-// Per-particle CTAs (box scans, link fill) are wide while fewer particles than this are in flight
-// (4 CTAs per SM of a 152-SM GB300) and narrow beyond; the results do not depend on the width.
+// Per-particle CTAs (marking, link fill, new-fluid detection) are LINK_WIDE threads while fewer
+// particles than this are in flight (4 CTAs per SM of a 152-SM GB300) and LINK_NARROW beyond; the
+// results do not depend on the width.
 constexpr int PARTICLES_WIDE = 4 * 152;
-inline int box_threads(int particles) { return particles < PARTICLES_WIDE ? 512 : 128; }
 
 constexpr int CONTACT_WARPS = 4;   // particles per 128-thread CTA, one warp each
 
@@ -516,46 +830,46 @@ __global__ void k_update(const Phys ph, const PartBuffers pb)
 // ------------------------------------------------------------------------------------------------
 // Solid marking over all particles (links.cu:25-48, 160-188).
 // ------------------------------------------------------------------------------------------------
-__device__ __forceinline__ void mark_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                                          int *owner, int p)
+template <int NT>
+__device__ __forceinline__ void mark_body(const Geo &geo, const Phys &ph, const PartBuffers &pb, int *owner, int p,
+                                          ShellRows<NT> &sr)
 {
-    const double *st = pb.state;
-    const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
-    const double r = ph.radius;
-    const double rsq = dmul(r, r);
-    const Box b = sphere_box(geo, px, py, pz, r, 0);
+    const PGeo &pg = pb.pgeo[p];
+    const Box b = pgeo_box(pg.mbox);
     if (b.x0 > b.x1 || b.y0 > b.y1 || b.z0 > b.z1) return;
-    const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
-    const int total = nx * ny * nz;
     // Single-precision classification away from the surface, the exact FP64 predicate in a band
-    // around it.  The band half-width bounds the float error of |x - X|^2 (coordinate rounding
-    // ~6e-8 |X| per component, arithmetic rounding ~1e-7 relative), so every node is classified
-    // exactly as the FP64 test classifies it.
-    const float pxf = (float)px, pyf = (float)py, pzf = (float)pz, rf2 = (float)rsq;
-    const float amax = fmaxf(fabsf(pxf), fmaxf(fabsf(pyf), fabsf(pzf)));
-    const float band = 1.0e-3f * rf2 + 1.0e-5f * (amax + 1.0f) * ((float)r + 2.0f) + 1.0e-3f;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int lz = t / (nx * ny);
-        const int rem = t - lz * nx * ny;
-        const int ly = rem / nx;
-        const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
+    // around it (PGeo::band bounds the float error), so every node is classified exactly as the
+    // FP64 test classifies it.
+    const float pxf = pg.c[0], pyf = pg.c[1], pzf = pg.c[2], rf2 = pg.rf2, band = pg.band;
+    // the ball |x - X|^2 <= r^2 + band (plus a margin for the row arithmetic)
+    for_shell_nodes<NT>(sr, b, pxf, pyf, pzf, 0.0f, sqrtf(rf2 + band) + 0.01f, [&](int ix, int iy, int iz) {
         const float fx = ((float)ix + 0.5f) - pxf, fy = ((float)iy + 0.5f) - pyf, fz = ((float)iz + 0.5f) - pzf;
         const float d2 = fx * fx + fy * fy + fz * fz;
-        if (d2 > rf2 + band) continue;
+        if (d2 > rf2 + band) return;
         if (d2 >= rf2 - band) {
+            const double *st = pb.state;
+            const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
             const double dx = dsub((double)ix + 0.5, px);
             const double dy = dsub((double)iy + 0.5, py);
             const double dz = dsub((double)iz + 0.5, pz);
-            if (sq3(dx, dy, dz) > rsq) continue;
+            if (sq3(dx, dy, dz) > dmul(ph.radius, ph.radius)) return;
         }
         const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
         atomicMin(reinterpret_cast<unsigned int *>(owner) + idx, (unsigned int)p);
-    }
+    });
 }
 
-__global__ void k_mark(const Geo geo, const Phys ph, const PartBuffers pb, int *owner)
+__global__ void k_pgeo(const Geo geo, const Phys ph, const PartBuffers pb)
 {
-    mark_body(geo, ph, pb, owner, blockIdx.x);
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < pb.np) pgeo_body(geo, ph, pb, p);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_mark(const Geo geo, const Phys ph, const PartBuffers pb, int *owner)
+{
+    __shared__ ShellRows<NT> sr;
+    mark_body<NT>(geo, ph, pb, owner, blockIdx.x, sr);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -577,42 +891,14 @@ constexpr int LINK_WIDE = 512, LINK_NARROW = 128;
 // (y, z) rows of the shell table (larger boxes scan the whole box)
 template <int NT> constexpr int link_max_rows() { return NT >= 512 ? 2048 : 1024; }
 
-template <int NT>
-__device__ __forceinline__ int block_exclusive_scan(int v, int *wsum, int &total)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int incl = v;
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, incl, off);
-        if (lane >= off) incl += t;
-    }
-    if (lane == 31) wsum[warp] = incl;
-    __syncthreads();
-    int wbase = 0, tot = 0;
-#pragma unroll
-    for (int k = 0; k < NT / 32; ++k) {
-        const int s = wsum[k];
-        if (k < warp) wbase += s;
-        tot += s;
-    }
-    __syncthreads();
-    total = tot;
-    return wbase + incl - v;
-}
 
 // Shared scratch of one link-fill CTA.
 template <int NT>
 struct LinkShared {
-    static constexpr int ROWS = link_max_rows<NT>();
-    int wsum[NT / 32];
+    ShellRows<NT> rows;       // shell table (its wsum also serves the chunk scans)
     unsigned mask[NT];        // candidate directions of each chunk node (bit ip)
     int scan[NT];             // exclusive prefix of the popcounts
     int node[NT];             // lattice index of each chunk node
-    int row_start[ROWS];      // shell table: first flat index of each (y, z) row
-    int row_xa[ROWS];         // start and length of the row's first x-interval
-    int row_na[ROWS];
-    int row_xb[ROWS];         // start of its second x-interval
 };
 
 template <bool F32Q, int NT>
@@ -620,11 +906,9 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
                                                const int *owner, DevStatus *status, int p, LinkShared<NT> &sm)
 {
     constexpr int LINK_THREADS = NT;
-    const double *st = pb.state;
-    const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
-    const double r = ph.radius;
-    const double rsq = dmul(r, r);
-    const Box b = sphere_box(geo, px, py, pz, r, 1);
+    const PGeo &pg = pb.pgeo[p];
+    const float r = (float)ph.radius;
+    const Box b = pgeo_box(pg.lbox);
     const long long slab = (long long)p * pb.link_cap;
     if (b.x0 > b.x1 || b.y0 > b.y1 || b.z0 > b.z1) {
         if (threadIdx.x == 0) pb.link_cnt[p] = 0;
@@ -632,53 +916,16 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
     }
     const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
     // conservative single-precision shell test: a link needs |x - X| <= r + sqrt(3)
-    const float reach = (float)r + 2.0f;
+    const float reach = r + 2.0f;
     const float reach2 = reach * reach;
-    const float pxf = (float)px, pyf = (float)py, pzf = (float)pz;
-    const int rows = ny * nz;
-    const bool use_rows = rows <= LinkShared<NT>::ROWS;
-    int total = nx * ny * nz;
-    if (use_rows) {
-        // shell rows: |x - X| in [r_in, r_out]; nodes closer than r_in are inside the sphere
-        const float r_out = reach + 0.01f, r_in = fmaxf((float)r - 0.05f, 0.0f);
-        int carry = 0;
-        for (int r0 = 0; r0 < rows; r0 += LINK_THREADS) {
-            const int row = r0 + threadIdx.x;
-            int cnt = 0;
-            if (row < rows) {
-                const int ly = row % ny, lz = row / ny;
-                const float dy = ((float)(b.y0 + ly) + 0.5f) - pyf, dz = ((float)(b.z0 + lz) + 0.5f) - pzf;
-                const float s2 = dy * dy + dz * dz;
-                int xa = 0, na = 0, xb = 0, nb = 0;
-                if (s2 <= r_out * r_out) {
-                    const float ho = sqrtf(r_out * r_out - s2);
-                    const int xl = max(b.x0, (int)ceilf(pxf - 0.5f - ho));
-                    const int xr = min(b.x1, (int)floorf(pxf - 0.5f + ho));
-                    if (s2 < r_in * r_in) {
-                        const float hi = sqrtf(r_in * r_in - s2);
-                        const int xle = (int)floorf(pxf - 0.5f - hi), xrs = (int)ceilf(pxf - 0.5f + hi);
-                        xa = xl;
-                        na = max(0, min(xr, xle) - xl + 1);
-                        xb = max(max(xl, xrs), xle + 1);   // never re-enter the first interval
-                        nb = max(0, xr - xb + 1);
-                    } else {
-                        xa = xl;
-                        na = max(0, xr - xl + 1);
-                    }
-                }
-                cnt = na + nb;
-                sm.row_xa[row] = xa;
-                sm.row_na[row] = na;
-                sm.row_xb[row] = xb;
-            }
-            int tot;
-            const int off = block_exclusive_scan<NT>(cnt, sm.wsum, tot);
-            if (row < rows) sm.row_start[row] = carry + off;
-            carry += tot;
-        }
-        total = carry;
-        __syncthreads();
-    }
+    const float pxf = pg.c[0], pyf = pg.c[1], pzf = pg.c[2];
+    // exact node-centre offsets for the float q: integer part of the centre and its fraction
+    const int ipx = pg.ic[0], ipy = pg.ic[1], ipz = pg.ic[2];
+    const float hx = pg.h[0], hy = pg.h[1], hz = pg.h[2];
+    // shell |x - X| in [r_in, r_out]: nodes closer than r_in are inside the sphere (solid)
+    int total = shell_rows_build<NT>(sm.rows, b, pxf, pyf, pzf, fmaxf(r - 0.05f, 0.0f), reach + 0.01f);
+    const bool use_rows = total >= 0;
+    if (!use_rows) total = nx * ny * nz;
     int base = 0;
     for (int c0 = 0; c0 < total; c0 += LINK_THREADS) {
         const int t = c0 + threadIdx.x;
@@ -687,16 +934,7 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
         if (t < total) {
             int ix, iy, iz;
             if (use_rows) {
-                int lo = 0, hi = rows - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (sm.row_start[mid] <= t) lo = mid;
-                    else hi = mid - 1;
-                }
-                const int o = t - sm.row_start[lo];
-                ix = o < sm.row_na[lo] ? sm.row_xa[lo] + o : sm.row_xb[lo] + (o - sm.row_na[lo]);
-                iy = b.y0 + lo % ny;
-                iz = b.z0 + lo / ny;
+                shell_rows_node<NT>(sm.rows, b, t, ix, iy, iz);
             } else {
                 const int lz = t / (nx * ny);
                 const int rem = t - lz * nx * ny;
@@ -722,7 +960,7 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
             my_node = (int)idx;
         }
         int ccount;
-        const int pos = block_exclusive_scan<NT>(__popc(mask), sm.wsum, ccount);
+        const int pos = block_exclusive_scan<NT>(__popc(mask), sm.rows.wsum, ccount);
         sm.mask[threadIdx.x] = mask;
         sm.scan[threadIdx.x] = pos;
         sm.node[threadIdx.x] = my_node;
@@ -749,16 +987,19 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
                 const int ix = node - iz * (int)geo.lxy - iy * geo.lx;
                 int r32 = -1;
                 if constexpr (F32Q)
-                    r32 = link_q_f32(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (float)((double)ix + 0.5 - px),
-                                     (float)((double)iy + 0.5 - py), (float)((double)iz + 0.5 - pz),
-                                     (float)rsq, q);
-                if (r32 > 0) ok = 1;
-                else
+                    r32 = link_q_f32(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (float)(ix - ipx) + hx,
+                                     (float)(iy - ipy) + hy, (float)(iz - ipz) + hz, pg.rf2, q);
+                if (r32 > 0) {
+                    ok = 1;
+                } else {
+                    const double *st = pb.state;
                     ok = link_q(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (double)ix + 0.5, (double)iy + 0.5,
-                                (double)iz + 0.5, px, py, pz, rsq, q) ? 1 : 0;
+                                (double)iz + 0.5, PCOL(st, pb.np, 0, p), PCOL(st, pb.np, 1, p),
+                                PCOL(st, pb.np, 2, p), dmul(ph.radius, ph.radius), q) ? 1 : 0;
+                }
             }
             int ltotal;
-            const int lpos = base + block_exclusive_scan<NT>(ok, sm.wsum, ltotal);
+            const int lpos = base + block_exclusive_scan<NT>(ok, sm.rows.wsum, ltotal);
             if (ok) {
                 if (lpos < pb.link_cap) {
                     pb.link_node[slab + lpos] = node;
@@ -786,39 +1027,41 @@ __global__ void __launch_bounds__(NT) k_link_fill(const Geo geo, const Phys ph, 
 // ------------------------------------------------------------------------------------------------
 // New-fluid detection (refill.cu:8-76), per particle around its new position.
 // ------------------------------------------------------------------------------------------------
+template <int NT>
 __device__ __forceinline__ void new_fluid_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
                                                const int *owner_prev, const int *owner_cur,
-                                               DevStatus *status, int p)
+                                               DevStatus *status, int p, ShellRows<NT> &sr)
 {
-    const double *st = pb.state;
-    const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
-    const double r = ph.radius;
-    const Box b = sphere_box(geo, px, py, pz, dadd(r, NEW_FLUID_THRESH), 1);
+    const PGeo &pg = pb.pgeo[p];
+    const Box b = pgeo_box(pg.nbox);
     if (b.x0 > b.x1 || b.y0 > b.y1 || b.z0 > b.z1) return;
-    const int nx = b.x1 - b.x0 + 1, ny = b.y1 - b.y0 + 1, nz = b.z1 - b.z0 + 1;
-    const int total = nx * ny * nz;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int lz = t / (nx * ny);
-        const int rem = t - lz * nx * ny;
-        const int ly = rem / nx;
-        const int ix = b.x0 + (rem - ly * nx), iy = b.y0 + ly, iz = b.z0 + lz;
+    const float rf = (float)ph.radius;
+    // candidates are fluid now (outside the sphere: nodes closer than r - 0.05 are solid) and
+    // within NEW_FLUID_THRESH of its surface
+    for_shell_nodes<NT>(sr, b, pg.c[0], pg.c[1], pg.c[2], fmaxf(rf - 0.05f, 0.0f),
+                        rf + (float)NEW_FLUID_THRESH + 0.01f, [&](int ix, int iy, int iz) {
         const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
-        if (owner_prev[idx] != p || owner_cur[idx] >= 0) continue;
+        if (owner_prev[idx] != p || owner_cur[idx] >= 0) return;
+        const double *st = pb.state;
+        const double px = PCOL(st, pb.np, 0, p), py = PCOL(st, pb.np, 1, p), pz = PCOL(st, pb.np, 2, p);
+        const double r = ph.radius;
         const double dx = dsub((double)ix + 0.5, px);
         const double dy = dsub((double)iy + 0.5, py);
         const double dz = dsub((double)iz + 0.5, pz);
         const double dist = __dsqrt_rn(sq3(dx, dy, dz));
-        if (dsub(dist, r) > NEW_FLUID_THRESH) continue;
+        if (dsub(dist, r) > NEW_FLUID_THRESH) return;
         const int slot = atomicAdd(&status->nf_count, 1);
         if (slot < pb.nf_cap) { pb.nf_node[slot] = (int)idx; pb.nf_pid[slot] = p; }
         else atomicOr(&status->nf_overflow, 1);
-    }
+    });
 }
 
-__global__ void k_new_fluid(const Geo geo, const Phys ph, const PartBuffers pb,
-                            const int *owner_prev, const int *owner_cur, DevStatus *status)
+template <int NT>
+__global__ void __launch_bounds__(NT) k_new_fluid(const Geo geo, const Phys ph, const PartBuffers pb,
+                                                  const int *owner_prev, const int *owner_cur, DevStatus *status)
 {
-    new_fluid_body(geo, ph, pb, owner_prev, owner_cur, status, blockIdx.x);
+    __shared__ ShellRows<NT> sr;
+    new_fluid_body<NT>(geo, ph, pb, owner_prev, owner_cur, status, blockIdx.x, sr);
 }
 
 // Refill values (refill.cu:78-240): one warp per new-fluid node, lane ip computes population ip
@@ -1058,7 +1301,9 @@ cudaError_t launch_mark(const Geo &geo, const Phys &ph, const PartBuffers &pb, i
     cudaError_t e = cudaMemsetAsync(owner_out, 0xFF, sizeof(int) * (size_t)geo.L, st);
     if (e) return e;
     if (pb.np <= 0) return cudaSuccess;
-    k_mark<<<pb.np, box_threads(pb.np), 0, st>>>(geo, ph, pb, owner_out);
+    k_pgeo<<<(pb.np + 127) / 128, 128, 0, st>>>(geo, ph, pb);
+    if (pb.np < PARTICLES_WIDE) k_mark<LINK_WIDE><<<pb.np, LINK_WIDE, 0, st>>>(geo, ph, pb, owner_out);
+    else k_mark<LINK_NARROW><<<pb.np, LINK_NARROW, 0, st>>>(geo, ph, pb, owner_out);
     return cudaGetLastError();
 }
 
@@ -1092,7 +1337,10 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
     if (pb.np <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(&status->nf_count, 0, sizeof(int), st);
     if (e) return e;
-    k_new_fluid<<<pb.np, box_threads(pb.np), 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
+    if (pb.np < PARTICLES_WIDE)
+        k_new_fluid<LINK_WIDE><<<pb.np, LINK_WIDE, 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
+    else
+        k_new_fluid<LINK_NARROW><<<pb.np, LINK_NARROW, 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
     RBTP_MODE_DISPATCH(mode, (k_refill_compute<M><<<152, 256, 0, st>>>(geo, ph, pb, owner_prev, f, g, status)));
     RBTP_MODE_DISPATCH(mode, (k_refill_scatter<M><<<152, 256, 0, st>>>(geo, ph, pb, f, g, faux, rho_wall, macros, rho, ux, uy, uz, phi, status)));
     return cudaGetLastError();
@@ -1206,14 +1454,28 @@ __global__ void k_owner_fill_b(const CavDesc *desc, const int *pmem)
         o[i] = -1;
 }
 
-__global__ void k_mark_b(const CavDesc *desc, const int2 *pmap)
+__global__ void k_pgeo_b(const CavDesc *desc, const int2 *pmap, int total)
 {
     pdl_wait();
     pdl_trigger();
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    const int2 mp = pmap[g];
+    const CavDesc &d = desc[mp.x];
+    if (d.out == OUT_IDLE) return;
+    pgeo_body(d.geo, d.ph, d.pb, mp.y);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_mark_b(const CavDesc *desc, const int2 *pmap)
+{
+    pdl_wait();
+    pdl_trigger();
+    __shared__ ShellRows<NT> sr;
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
     if (d.out == OUT_IDLE) return;
-    mark_body(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], mp.y);
+    mark_body<NT>(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], mp.y, sr);
 }
 
 template <bool F32Q, int NT>
@@ -1228,14 +1490,16 @@ __global__ void __launch_bounds__(NT) k_link_fill_b(const CavDesc *desc, const i
     link_fill_body<F32Q, NT>(d.geo, d.ph, d.pb, d.owner[d.ocur ^ 1], d.status, mp.y, sm);
 }
 
-__global__ void k_new_fluid_b(const CavDesc *desc, const int2 *pmap)
+template <int NT>
+__global__ void __launch_bounds__(NT) k_new_fluid_b(const CavDesc *desc, const int2 *pmap)
 {
     pdl_wait();
     pdl_trigger();
+    __shared__ ShellRows<NT> sr;
     const int2 mp = pmap[blockIdx.x];
     const CavDesc &d = desc[mp.x];
     if (d.out == OUT_IDLE) return;
-    new_fluid_body(d.geo, d.ph, d.pb, d.owner[d.ocur], d.owner[d.ocur ^ 1], d.status, mp.y);
+    new_fluid_body<NT>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.owner[d.ocur ^ 1], d.status, mp.y, sr);
 }
 
 template <int MODE>
@@ -1283,12 +1547,16 @@ cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int to
              desc, pmap, total);
     RBTP_PDL(k_update_b, dim3(bl), dim3(t), st, desc, pmap, total);
     RBTP_PDL(k_owner_fill_b, dim3(64, npmem), dim3(256), st, desc, pmem);
-    RBTP_PDL(k_mark_b, dim3(total), dim3(box_threads(total)), st, desc, pmap);
-    if (total < PARTICLES_WIDE)
+    RBTP_PDL(k_pgeo_b, dim3(bl), dim3(t), st, desc, pmap, total);
+    if (total < PARTICLES_WIDE) {
+        RBTP_PDL(k_mark_b<LINK_WIDE>, dim3(total), dim3(LINK_WIDE), st, desc, pmap);
         RBTP_PDL(k_link_fill_b<MODE != RBTP_STORE_F64, LINK_WIDE>, dim3(total), dim3(LINK_WIDE), st, desc, pmap);
-    else
+        RBTP_PDL(k_new_fluid_b<LINK_WIDE>, dim3(total), dim3(LINK_WIDE), st, desc, pmap);
+    } else {
+        RBTP_PDL(k_mark_b<LINK_NARROW>, dim3(total), dim3(LINK_NARROW), st, desc, pmap);
         RBTP_PDL(k_link_fill_b<MODE != RBTP_STORE_F64, LINK_NARROW>, dim3(total), dim3(LINK_NARROW), st, desc, pmap);
-    RBTP_PDL(k_new_fluid_b, dim3(total), dim3(box_threads(total)), st, desc, pmap);
+        RBTP_PDL(k_new_fluid_b<LINK_NARROW>, dim3(total), dim3(LINK_NARROW), st, desc, pmap);
+    }
     RBTP_PDL(k_refill_compute_b<MODE>, dim3(8, npmem), dim3(256), st, desc, pmem);
     RBTP_PDL(k_refill_scatter_b<MODE>, dim3(8, npmem), dim3(256), st, desc, pmem);
 #undef RBTP_PDL

@@ -102,6 +102,15 @@ __device__ __forceinline__ double dweight_rt(int i)
 {
     return i == 0 ? 8.0 / 27.0 : (i <= 6 ? 2.0 / 27.0 : (i <= 18 ? 1.0 / 54.0 : 1.0 / 216.0));
 }
+// the same weights and their inverses rounded to float (the float storage modes' factors)
+__device__ __forceinline__ float fweight_rt(int i)
+{
+    return i == 0 ? (float)(8.0 / 27.0) : (i <= 6 ? (float)(2.0 / 27.0) : (i <= 18 ? (float)(1.0 / 54.0) : (float)(1.0 / 216.0)));
+}
+__device__ __forceinline__ float finvweight_rt(int i)
+{
+    return i == 0 ? (float)(27.0 / 8.0) : (i <= 6 ? (float)(27.0 / 2.0) : (i <= 18 ? 54.0f : 216.0f));
+}
 
 template <class F, int... Is>
 __host__ __device__ __forceinline__ void unroll_impl(F &&f, std::integer_sequence<int, Is...>)
@@ -283,11 +292,26 @@ constexpr int ibb_chunks_for(long long link_cap)
     return link_cap <= 2048 ? 1 : (link_cap >= 2048LL * IBB_CHUNKS ? IBB_CHUNKS : (int)((link_cap + 2047) / 2048));
 }
 
+// Per-particle geometry derived once per link build from the FP64 position (one thread per
+// particle), so that the per-particle CTAs spend no FP64 work on their setup: the integer boxes of
+// marking (radius r), link fill (r, padded by 1) and new-fluid detection (r + 1.76..., padded by 1),
+// the integer part of the centre and 1/2 minus its fraction (exact float node offsets), the centre
+// in float, the float constants of the marking band, and the rigid-body velocity, spin and
+// temperature in float for the next IBB pass (they change only in the integrator, before the build).
+struct PGeo {
+    int mbox[6], lbox[6], nbox[6];   // x0, x1, y0, y1, z0, z1
+    int ic[3];
+    float h[3], c[3];
+    float rf2, band;
+    float v[3], w[3], T, momk, t0;   // velocity, spin, temperature; 2 rho0 / c_s^2; T_REF
+};
+
 struct PartBuffers {
     int np;
     double *state;          // 33 columns x np, column-major (col c at state + c*np)
     double *hpart;          // IBB partial sums: np x IBB_CHUNKS x 7 (force, torque, heat)
     int ibb_chunks;         // link chunks (CTAs) per particle, 1..IBB_CHUNKS, from the link capacity
+    PGeo *pgeo;             // np entries, refreshed before every marking pass
     double *cF;             // contact force (3*np)
     int *owner_cur, *owner_new;   // solid owner maps (L each); -1 = fluid
     int link_cap;           // links per particle slab
