@@ -277,8 +277,14 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
     const size_t sb = store_bytes(h->mode);
     const size_t P = (size_t)27 * (size_t)L;
     for (int k = 0; k < 2; ++k) {
-        CKC(cudaMalloc(&h->f[k], P * sb));
-        CKC(cudaMalloc(&h->g[k], P * sb));
+        if (h->mode == RBTP_STORE_F64) {
+            CKC(cudaMalloc(&h->f[k], P * sb));
+            CKC(cudaMalloc(&h->g[k], P * sb));
+        } else {
+            // paired (f_i, g_i) slots: f and g are the same allocation
+            CKC(cudaMalloc(&h->f[k], 2 * P * sb));
+            h->g[k] = h->f[k];
+        }
     }
     CKC(dalloc(&h->faux, L));
     CKC(dalloc(&h->rho_wall, 2 * (size_t)cfg->ly * cfg->lz));
@@ -347,7 +353,11 @@ int rbtp_destroy(rbtp_handle *h)
     if (!h) return RBTP_OK;
     rbtp_batch_detach(h);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    for (int k = 0; k < 2; ++k) { cudaFree(h->f[k]); cudaFree(h->g[k]); cudaFree(h->owner[k]); }
+    for (int k = 0; k < 2; ++k) {
+        if (h->g[k] != h->f[k]) cudaFree(h->g[k]);
+        cudaFree(h->f[k]);
+        cudaFree(h->owner[k]);
+    }
     cudaFree(h->faux); cudaFree(h->rho_wall);
     cudaFree(h->rho); cudaFree(h->ux); cudaFree(h->uy); cudaFree(h->uz); cudaFree(h->phi);
     cudaFree(h->ted); cudaFree(h->ked); cudaFree(h->fcol); cudaFree(h->gcol);
@@ -1098,8 +1108,12 @@ int rbtp_checkpoint_write(rbtp_handle *h, const char *path)
     if (!fp) return fail(h, RBTP_ERR_IO, std::string("cannot open ") + path);
     bool ok = std::fwrite(CKP_MAGIC, 1, 8, fp) == 8 && std::fwrite(&hd, sizeof(hd), 1, fp) == 1 &&
               std::fwrite(&h->cfg, sizeof(rbtp_config), 1, fp) == 1;
+    // 2P bytes of populations: f then g (FP64), or the paired (f_i, g_i) slots (float modes)
+    const bool paired = h->g[h->cur] == h->f[h->cur];
     for (int k = 0; ok && k < 2; ++k) {
-        if (cudaMemcpy(pop.data(), k == 0 ? h->f[h->cur] : h->g[h->cur], P, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        const char *src = paired ? static_cast<const char *>(h->f[h->cur]) + k * P
+                                 : static_cast<const char *>(k == 0 ? h->f[h->cur] : h->g[h->cur]);
+        if (cudaMemcpy(pop.data(), src, P, cudaMemcpyDeviceToHost) != cudaSuccess) {
             std::fclose(fp);
             return fail(h, RBTP_ERR_CUDA, "checkpoint read-back failed");
         }
@@ -1160,8 +1174,13 @@ int rbtp_checkpoint_read(rbtp_handle *h, const char *path)
                       std::fread(prow.data(), sizeof(double), prow.size(), fp) == prow.size();
     std::fclose(fp);
     if (!body) return fail(h, RBTP_ERR_IO, std::string("checkpoint is truncated: ") + path);
-    CK(cudaMemcpyAsync(h->f[0], f.data(), P, cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->g[0], g.data(), P, cudaMemcpyHostToDevice, h->stream));
+    if (h->g[0] == h->f[0]) {   // paired (f_i, g_i) slots: the 2P bytes in file order
+        CK(cudaMemcpyAsync(h->f[0], f.data(), P, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(static_cast<char *>(h->f[0]) + P, g.data(), P, cudaMemcpyHostToDevice, h->stream));
+    } else {
+        CK(cudaMemcpyAsync(h->f[0], f.data(), P, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->g[0], g.data(), P, cudaMemcpyHostToDevice, h->stream));
+    }
     CK(cudaMemcpyAsync(h->faux, aux.data(), L * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->rho_wall, wall.data(), W * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (hd.macros_valid) {

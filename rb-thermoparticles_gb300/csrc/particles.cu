@@ -469,13 +469,14 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
             const int o = dopp_rt(ip);
             const float wr = fweight_rt(ip), winv = finvweight_rt(ip);   // w_opp = w_ip
+            // (f_i, g_i) slots of the paired layout
             auto ldf = [&](const S *ptr) -> float {
-                if constexpr (MODE == RBTP_STORE_F16S) return __half2float(*ptr) * wr;
-                else return (float)*ptr;
+                if constexpr (MODE == RBTP_STORE_F16S) return __low2float(*ptr) * wr;
+                else return ptr->x;
             };
             auto ldg = [&](const S *ptr) -> float {
-                if constexpr (MODE == RBTP_STORE_F16S) return (__half2float(*ptr) + t0f) * wr;
-                else return (float)*ptr;
+                if constexpr (MODE == RBTP_STORE_F16S) return (__high2float(*ptr) + t0f) * wr;
+                else return ptr->y;
             };
             // moving wall velocity at the intersection point (ibb.cu:33-46)
             const float relx = ((float)(ix - ipx) + hx) + q * (float)cxi;
@@ -523,18 +524,16 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             // The population that streams into x along opp comes from the solid node x + c_ip: the
             // pull of the next step reads it from slot (opp, x + c_ip).
             const long long solid = (long long)x + cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
+            // one slot holds both populations (f and g buffers are the same allocation)
             S *fs = fB + (long long)o * L + solid;
-            S *gs = gB + (long long)o * L + solid;
             float f_out = fval, g_out = gval;
             if constexpr (MODE == RBTP_STORE_F16S) {
                 // the value the reference would read back is the rounded one
-                *fs = __float2half_rn(fval * winv);
-                *gs = __float2half_rn(gval * winv - t0f);
+                *fs = __floats2half2_rn(fval * winv, gval * winv - t0f);
                 f_out = ldf(fs);
-                g_out = ldg(gs);
+                g_out = ldg(fs);
             } else {
-                *fs = fval;
-                *gs = gval;
+                *fs = make_float2(fval, gval);
             }
             // ibb.cu:160-187 (force, torque about the same intersection point) and 202-204 (heat)
             const float Fx = ((float)cxi - uwx) * f_here - ((float)-cxi - uwx) * f_out;

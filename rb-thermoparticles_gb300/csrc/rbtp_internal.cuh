@@ -127,39 +127,47 @@ __host__ __device__ __forceinline__ void unroll(F &&f)
 // Population storage modes.  R is the arithmetic type of the collision, S the storage type.
 // FP16 mode stores (pop / w_i) for f (the deviation-form f needs no shift) and (g / w_i - T0) for g.
 // ------------------------------------------------------------------------------------------------
+// Population storage.  FP64 keeps f and g in two arrays of 27 L doubles ([ip][z][y][x], the
+// reference layout).  The FP32 and shifted-FP16 modes pair the two distributions per slot: one
+// array of 27 L (f_i, g_i) pairs (float2 / __half2, [ip][z][y][x]), so that a gather or a store
+// of both populations of a direction is one 8- or 4-byte access; the f and g buffer pointers of
+// such a handle are the same allocation, and ld_f/ld_g/st_f/st_g address the halves of a slot.
 template <int MODE> struct Store;
 template <> struct Store<RBTP_STORE_F64> {
     using S = double;
     using R = double;
+    static constexpr bool PAIRED = false;
     static __device__ __forceinline__ R ld_f(const S *p, double, double) { return *p; }
     static __device__ __forceinline__ R ld_g(const S *p, double, double) { return *p; }
     static __device__ __forceinline__ void st_f(S *p, R v, double, double) { *p = v; }
     static __device__ __forceinline__ void st_g(S *p, R v, double, double) { *p = v; }
 };
 template <> struct Store<RBTP_STORE_F32> {
-    using S = float;
+    using S = float2;   // (f_i, g_i)
     using R = float;
-    static __device__ __forceinline__ R ld_f(const S *p, double, double) { return *p; }
-    static __device__ __forceinline__ R ld_g(const S *p, double, double) { return *p; }
-    static __device__ __forceinline__ void st_f(S *p, R v, double, double) { *p = v; }
-    static __device__ __forceinline__ void st_g(S *p, R v, double, double) { *p = v; }
+    static constexpr bool PAIRED = true;
+    static __device__ __forceinline__ R ld_f(const S *p, double, double) { return p->x; }
+    static __device__ __forceinline__ R ld_g(const S *p, double, double) { return p->y; }
+    static __device__ __forceinline__ void st_f(S *p, R v, double, double) { p->x = v; }
+    static __device__ __forceinline__ void st_g(S *p, R v, double, double) { p->y = v; }
 };
 template <> struct Store<RBTP_STORE_F16S> {
-    using S = __half;
+    using S = __half2;  // (f_i / w_i, g_i / w_i - T0)
     using R = float;
+    static constexpr bool PAIRED = true;
     // w: lattice weight of the slot's direction, t0: reference temperature (g shift)
-    static __device__ __forceinline__ R ld_f(const S *p, double w, double) { return __half2float(*p) * (float)w; }
+    static __device__ __forceinline__ R ld_f(const S *p, double w, double) { return __low2float(*p) * (float)w; }
     static __device__ __forceinline__ R ld_g(const S *p, double w, double t0)
     {
-        return (__half2float(*p) + (float)t0) * (float)w;
+        return (__high2float(*p) + (float)t0) * (float)w;
     }
     static __device__ __forceinline__ void st_f(S *p, R v, double w, double)
     {
-        *p = __float2half_rn(v * (float)(1.0 / w));
+        reinterpret_cast<__half *>(p)[0] = __float2half_rn(v * (float)(1.0 / w));
     }
     static __device__ __forceinline__ void st_g(S *p, R v, double w, double t0)
     {
-        *p = __float2half_rn(v * (float)(1.0 / w) - (float)t0);
+        reinterpret_cast<__half *>(p)[1] = __float2half_rn(v * (float)(1.0 / w) - (float)t0);
     }
 };
 

@@ -43,13 +43,17 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     // lattice-weight class, and the collision constants are divided by w_i (no per-population
     // scaling on load or store).  The other modes work on f_i and g_i.
     constexpr bool SC = MODE == RBTP_STORE_F16S;
-    auto ldf = [&](const S *p, double w) -> R {
-        if constexpr (SC) return (R)__half2float(*reinterpret_cast<const __half *>(p));
-        else return ST::ld_f(p, w, t0);
-    };
-    auto ldg = [&](const S *p, double w) -> R {
-        if constexpr (SC) return (R)__half2float(*reinterpret_cast<const __half *>(p));
-        else return ST::ld_g(p, w, t0);
+    // both populations of a slot (one access in the paired layouts of the float modes)
+    auto ldfg = [&](const S *p, double w, R &fv, R &gv) {
+        if constexpr (SC) {
+            const __half2 v = *p;
+            fv = __low2float(v);
+            gv = __high2float(v);
+        } else if constexpr (ST::PAIRED) {
+            const float2 v = *p;
+            fv = v.x;
+            gv = v.y;
+        }
     };
     R f[27], g[27];
     unroll<27>([&](auto I) {
@@ -57,16 +61,24 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
         constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i), o = dopp(i);
         constexpr double w = dweight(i);
         if constexpr (!PULL || i == 0) {
-            f[i] = ldf(fin + (long long)i * L + node, w);
-            g[i] = ldg(gin + (long long)i * L + node, w);
+            if constexpr (ST::PAIRED) {
+                ldfg(fin + (long long)i * L + node, w, f[i], g[i]);
+            } else {
+                f[i] = ST::ld_f(fin + (long long)i * L + node, w, t0);
+                g[i] = ST::ld_g(gin + (long long)i * L + node, w, t0);
+            }
         } else {
             // f_i(x) = f*_i(x - c_i); a neighbour outside the box returns f*_opp(x) (bounce-back)
             const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
                              (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
             const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
             const long long src = out ? ((long long)o * L + node) : ((long long)i * L + node - off);
-            f[i] = ldf(fin + src, w);
-            g[i] = ldg(gin + src, w);
+            if constexpr (ST::PAIRED) {
+                ldfg(fin + src, w, f[i], g[i]);
+            } else {
+                f[i] = ST::ld_f(fin + src, w, t0);
+                g[i] = ST::ld_g(gin + src, w, t0);
+            }
         }
     });
     if constexpr (PULL) {
@@ -243,15 +255,18 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
         constexpr int i = decltype(I)::value;
         constexpr double w = dweight(i);
         if constexpr (SC) {
-            *reinterpret_cast<__half *>(fout + (long long)i * L + node) = __float2half_rn(f[i]);
-            *reinterpret_cast<__half *>(gout + (long long)i * L + node) = __float2half_rn(g[i]);
+            fout[(long long)i * L + node] = __floats2half2_rn(f[i], g[i]);
             if constexpr (OUT == OUT_MACROS_COL) {
                 b.fcol[(long long)i * L + node] = (double)((R)w * f[i]);
                 b.gcol[(long long)i * L + node] = (double)((R)w * (g[i] + K.t0));
             }
         } else {
-            ST::st_f(fout + (long long)i * L + node, f[i], w, t0);
-            ST::st_g(gout + (long long)i * L + node, g[i], w, t0);
+            if constexpr (ST::PAIRED) {
+                fout[(long long)i * L + node] = make_float2(f[i], g[i]);
+            } else {
+                ST::st_f(fout + (long long)i * L + node, f[i], w, t0);
+                ST::st_g(gout + (long long)i * L + node, g[i], w, t0);
+            }
             if constexpr (OUT == OUT_MACROS_COL) {
                 b.fcol[(long long)i * L + node] = (double)f[i];
                 b.gcol[(long long)i * L + node] = (double)g[i];
