@@ -353,6 +353,37 @@ def nu_accuracy(steps: int = 60000, every: int = 100) -> dict:
     for name in ("f64_seed2", "f32", "f16s"):
         out[name]["rel_err_vs_f64"] = {k: abs(out[name][k] / out["f64"][k] - 1.0)
                                        for k in ("nu_bulk", "nu_top", "nu_bottom")}
+    out["steady"] = nu_accuracy_steady()
+    return out
+
+
+def nu_accuracy_steady(steps: int = 60000, every: int = 500) -> dict:
+    """Time-averaged Nusselt numbers of FP32 and shifted-FP16 storage against FP64 on steady
+    convection (64x64x32, Ra=3e4, Pr=0.71, seeded +-1e-2 start; one steady roll after ~30k steps),
+    where no chaotic noise floor blurs the comparison; average over the last third."""
+    import numpy as np
+    from rbtp import Solver, workloads as W
+    out = {"workload": "64x64x32 Ra=3e4 Pr=0.71 (steady convection), seeded +-1e-2 start",
+           "steps": steps, "sample_every": every, "average_over": "last 1/3 of the run"}
+    series = {}
+    for st, name in ((0, "f64"), (1, "f32"), (2, "f16s")):
+        cfg = W.config("plain_fp64", rayleigh=3e4, storage=st)
+        s = Solver(cfg)
+        s.load_state(*W.initial_state(cfg, seed=1, amp=1e-2))
+        rows = []
+        for _ in range(steps // every):
+            s.step(every, macros_last=True)
+            rows.append(s.nu(s.istep))
+        series[name] = np.array(rows)
+        s.close()
+    keep = slice(2 * len(series["f64"]) // 3, None)
+    for name in series:
+        r = series[name][keep]
+        out[name] = {"nu_bulk": float(r[:, 2].mean()), "nu_top": float(r[:, 3].mean()),
+                     "nu_bottom": float(r[:, 4].mean())}
+    for name in ("f32", "f16s"):
+        out[name]["rel_err_vs_f64"] = {k: abs(out[name][k] / out["f64"][k] - 1.0)
+                                       for k in ("nu_bulk", "nu_top", "nu_bottom")}
     return out
 
 

@@ -254,6 +254,8 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
     Phys &ph = h->ph;
     ph.tau = h->der.tau; ph.tauc = h->der.tauc; ph.grav0 = h->der.grav0; ph.beta = cfg->beta;
     ph.thot = cfg->t_hot; ph.tcold = cfg->t_cold; ph.t0 = cfg->t_ref; ph.diff = h->der.diff;
+    ph.tlb = -(cfg->t_hot - cfg->t_cold) / (double)cfg->lx;   // conduction profile, node centres
+    ph.tla = cfg->t_hot + 0.5 * ph.tlb;
     ph.visc = cfg->visc; ph.rho0 = cfg->rho0;
     ph.radius = h->der.particle_radius; ph.mass = h->der.particle_mass;
     ph.inertia = h->der.particle_inertia; ph.heat_cap = h->der.particle_heat_capacity;

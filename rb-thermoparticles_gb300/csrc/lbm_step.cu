@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(128) k_stream_export(const Geo geo, const Phys
         const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
         const long long src = out ? ((long long)o * L + node) : ((long long)i * L + node - off);
         fout[(long long)i * L + node] = (double)ST::ld_f(fin + src, w, ph.t0);
-        double gr = (double)ST::ld_g(gin + src, w, ph.t0);
+        double gr = (double)ST::ld_g(gin + src, w, gshift(ph, out ? ix : ix - cx));
         if (ox && !oy && !oz) {
             const double tw = (cx == 1) ? ph.thot : ph.tcold;
             gr = wall_image(gr, w, tw, rw);
@@ -96,11 +96,12 @@ __global__ void k_home_export(const Geo geo, const Phys ph, const void *fin_, co
     if (n >= geo.L) return;
     const S *fin = static_cast<const S *>(fin_);
     const S *gin = static_cast<const S *>(gin_);
+    const double sh = gshift(ph, (int)(n % geo.lx));
     unroll<27>([&](auto I) {
         constexpr int i = decltype(I)::value;
         constexpr double w = dweight(i);
         fout[(long long)i * geo.L + n] = (double)ST::ld_f(fin + (long long)i * geo.L + n, w, ph.t0);
-        gout[(long long)i * geo.L + n] = (double)ST::ld_g(gin + (long long)i * geo.L + n, w, ph.t0);
+        gout[(long long)i * geo.L + n] = (double)ST::ld_g(gin + (long long)i * geo.L + n, w, sh);
     });
 }
 
@@ -115,11 +116,12 @@ __global__ void k_home_import(const Geo geo, const Phys ph, const double *fin, c
     if (n >= geo.L) return;
     S *fout = static_cast<S *>(fout_);
     S *gout = static_cast<S *>(gout_);
+    const double sh = gshift(ph, (int)(n % geo.lx));
     unroll<27>([&](auto I) {
         constexpr int i = decltype(I)::value;
         constexpr double w = dweight(i);
         ST::st_f(fout + (long long)i * geo.L + n, (R)fin[(long long)i * geo.L + n], w, ph.t0);
-        ST::st_g(gout + (long long)i * geo.L + n, (R)gin[(long long)i * geo.L + n], w, ph.t0);
+        ST::st_g(gout + (long long)i * geo.L + n, (R)gin[(long long)i * geo.L + n], w, sh);
     });
 }
 
@@ -150,7 +152,7 @@ __global__ void k_fresh_init(const Geo geo, const Phys ph, void *f_, void *g_, d
         if (i == 0) geq -= lambda0 * tT * r;
         else geq += w * tT * r;
         ST::st_f(f + (long long)i * geo.L + n, (R)(w * (0.0 + 0.0 + 0.5 * (0.0 - 0.0))), w, ph.t0);
-        ST::st_g(g + (long long)i * geo.L + n, (R)geq, w, ph.t0);
+        ST::st_g(g + (long long)i * geo.L + n, (R)geq, w, gshift(ph, (int)(n % geo.lx)));
     });
 }
 

@@ -140,7 +140,6 @@ __device__ __forceinline__ void pgeo_body(const Geo &geo, const Phys &ph, const 
     }
     g.T = (float)PCOL(st, pb.np, 30, p);
     g.momk = (float)(2.0 * ph.rho0 * 3.0);
-    g.t0 = (float)ph.t0;
     pb.pgeo[p] = g;
 }
 
@@ -453,7 +452,8 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
         const float vxf = pg.v[0], vyf = pg.v[1], vzf = pg.v[2];
         const float wxf = pg.w[0], wyf = pg.w[1], wzf = pg.w[2];
         const float mom_k = pg.momk;   // 2 rho0 / c_s^2
-        const float Tpf = pg.T, t0f = pg.t0;
+        const float Tpf = pg.T;
+        const float tla = ph.kf.tla, tlb = ph.kf.tlb;   // conduction profile (shifted FP16 g)
         df sum[7];
 #pragma unroll
         for (int k = 0; k < 7; ++k) sum[k] = df{0.0f, 0.0f};
@@ -474,8 +474,9 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
                 if constexpr (MODE == RBTP_STORE_F16S) return __low2float(*ptr) * wr;
                 else return ptr->x;
             };
-            auto ldg = [&](const S *ptr) -> float {
-                if constexpr (MODE == RBTP_STORE_F16S) return (__high2float(*ptr) + t0f) * wr;
+            // shifted-FP16 g holds g / w - T_c(x_home): the slot's home node x-index gives the shift
+            auto ldg = [&](const S *ptr, int ixh) -> float {
+                if constexpr (MODE == RBTP_STORE_F16S) return (__high2float(*ptr) + (tla + tlb * (float)ixh)) * wr;
                 else return ptr->y;
             };
             // moving wall velocity at the intersection point (ibb.cu:33-46)
@@ -495,7 +496,7 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const bool fluid1 = in1 && owner_cur[x1] < 0;
 
             const float f_here = ldf(fB + (long long)ip * L + x);
-            const float g_here = ldg(gB + (long long)ip * L + x);
+            const float g_here = ldg(gB + (long long)ip * L + x, ix);
             float fval, gval;
             // ibb.cu:52-73 (f: q < 0.5), ibb.cu:114-128 (g: q <= 0.5)
             if (fluid1) {
@@ -512,10 +513,10 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const float amp = 2.0f * wr * Tpf * (1.0f + (float)rho[x]);
             if (fluid1) {
                 if (q <= 0.5f) {
-                    const float gu = ldg(gB + (long long)ip * L + x1);
+                    const float gu = ldg(gB + (long long)ip * L + x1, ix1);
                     gval = -(2.0f * q * g_here + (1.0f - 2.0f * q) * gu) + amp;
                 } else {
-                    const float go = ldg(gB + (long long)o * L + x);
+                    const float go = ldg(gB + (long long)o * L + x, ix);
                     gval = -g_here * inv_2q + amp * inv_2q + (2.0f * q - 1.0f) * inv_2q * go;
                 }
             } else {
@@ -529,9 +530,10 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             float f_out = fval, g_out = gval;
             if constexpr (MODE == RBTP_STORE_F16S) {
                 // the value the reference would read back is the rounded one
-                *fs = __floats2half2_rn(fval * winv, gval * winv - t0f);
+                const int ixs = ix + cxi;   // home of the written slot: the solid node
+                *fs = __floats2half2_rn(fval * winv, gval * winv - (tla + tlb * (float)ixs));
                 f_out = ldf(fs);
-                g_out = ldg(fs);
+                g_out = ldg(fs, ixs);
             } else {
                 *fs = make_float2(fval, gval);
             }
@@ -1105,12 +1107,12 @@ __device__ __forceinline__ void refill_compute_body(const Geo &geo, const Phys &
                 const int x2 = ix + 2 * cx2, y2 = iy + 2 * cy2, z2 = iz + 2 * cz2;
                 const bool in2 = x2 >= 0 && x2 < geo.lx && y2 >= 0 && y2 < geo.ly && z2 >= 0 && z2 < geo.lz;
                 const double f1 = (double)ST::ld_f(fB + (long long)ip * L + i1, w, ph.t0);
-                const double g1 = (double)ST::ld_g(gB + (long long)ip * L + i1, w, ph.t0);
+                const double g1 = (double)ST::ld_g(gB + (long long)ip * L + i1, w, gshift(ph, x1));
                 if (in2) {
                     const long long i2 = (long long)z2 * geo.lxy + (long long)y2 * geo.lx + x2;
                     if (owner_prev[i2] < 0) {
                         tf += 2.0 * f1 - (double)ST::ld_f(fB + (long long)ip * L + i2, w, ph.t0);
-                        tg += 2.0 * g1 - (double)ST::ld_g(gB + (long long)ip * L + i2, w, ph.t0);
+                        tg += 2.0 * g1 - (double)ST::ld_g(gB + (long long)ip * L + i2, w, gshift(ph, x2));
                         ++sc;
                         continue;
                     }
@@ -1219,7 +1221,7 @@ __device__ __forceinline__ void refill_scatter_body(const Geo &geo, const Phys &
         if (!(ox || oy || oz)) {
             const long long src = (long long)idx - cx - (long long)cy * geo.lx - (long long)cz * geo.lxy;
             ST::st_f(fB + (long long)ip * L + src, (R)fv, w, ph.t0);
-            ST::st_g(gB + (long long)ip * L + src, (R)gv, w, ph.t0);
+            ST::st_g(gB + (long long)ip * L + src, (R)gv, w, gshift(ph, ix - cx));
         } else {
             ST::st_f(fB + (long long)o * L + idx, (R)fv, w, ph.t0);
             double gs = gv;
@@ -1229,7 +1231,7 @@ __device__ __forceinline__ void refill_scatter_body(const Geo &geo, const Phys &
                 const long long ws = (long long)iz * geo.ly + iy + (cx == 1 ? 0 : (long long)geo.lz * geo.ly);
                 gs = wall_image(gv, w, tw, rho_wall[ws]);
             }
-            ST::st_g(gB + (long long)o * L + idx, (R)gs, w, ph.t0);
+            ST::st_g(gB + (long long)o * L + idx, (R)gs, w, gshift(ph, ix));
         }
         if (ip == 0) {
             faux[idx] = 0.0;

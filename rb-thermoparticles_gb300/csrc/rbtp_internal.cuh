@@ -151,23 +151,26 @@ template <> struct Store<RBTP_STORE_F32> {
     static __device__ __forceinline__ void st_f(S *p, R v, double, double) { p->x = v; }
     static __device__ __forceinline__ void st_g(S *p, R v, double, double) { p->y = v; }
 };
+// Shifted FP16: f_i / w_i (f is already the deviation from rest) and g_i / w_i - T_c(x), T_c the
+// conduction profile (the thermal rest state) at the x of the slot's home node, so that FP16 holds
+// only the departure from conduction.  `shift` below is T_c(x_home) (gshift), ignored elsewhere.
 template <> struct Store<RBTP_STORE_F16S> {
-    using S = __half2;  // (f_i / w_i, g_i / w_i - T0)
+    using S = __half2;  // (f_i / w_i, g_i / w_i - T_c(x))
     using R = float;
     static constexpr bool PAIRED = true;
-    // w: lattice weight of the slot's direction, t0: reference temperature (g shift)
+    // w: lattice weight of the slot's direction
     static __device__ __forceinline__ R ld_f(const S *p, double w, double) { return __low2float(*p) * (float)w; }
-    static __device__ __forceinline__ R ld_g(const S *p, double w, double t0)
+    static __device__ __forceinline__ R ld_g(const S *p, double w, double shift)
     {
-        return (__high2float(*p) + (float)t0) * (float)w;
+        return (__high2float(*p) + (float)shift) * (float)w;
     }
     static __device__ __forceinline__ void st_f(S *p, R v, double w, double)
     {
         reinterpret_cast<__half *>(p)[0] = __float2half_rn(v * (float)(1.0 / w));
     }
-    static __device__ __forceinline__ void st_g(S *p, R v, double w, double t0)
+    static __device__ __forceinline__ void st_g(S *p, R v, double w, double shift)
     {
-        reinterpret_cast<__half *>(p)[1] = __float2half_rn(v * (float)(1.0 / w) - (float)t0);
+        reinterpret_cast<__half *>(p)[1] = __float2half_rn(v * (float)(1.0 / w) - (float)shift);
     }
 };
 
@@ -206,16 +209,21 @@ struct StepK {
     R gd0, Rc;         // 2 tauc / 3, 1 - 1/(2 tauc)          (collision.cu:72-73)
     R g0b, t0;         // grav0 * beta, T_REF                 (macrovar.cu:45)
     R thot, tcold;     // wall temperatures                   (streaming.cu:55-58)
+    R tla, tlb;        // conduction profile T_c(x) = tla + tlb x (shifted-FP16 g storage)
 };
 
 struct Phys {
     double tau, tauc, grav0, beta, thot, tcold, t0, diff, visc, rho0;
+    double tla, tlb;   // conduction profile at node x: T_c(x) = tla + tlb x
     StepK<double> kd;
     StepK<float> kf;
     double radius, mass, inertia, heat_cap, rho_ratio;
     double rep_coeff, min_gap, min_gap_w, stf0, stf1, stf0_w, stf1_w;
     double cp_ratio, vol_fraction;
 };
+
+// Shift of the shifted-FP16 g storage for a slot whose home node has x-index ix.
+__host__ __device__ __forceinline__ double gshift(const Phys &ph, int ix) { return ph.tla + ph.tlb * (double)ix; }
 
 template <class R>
 __host__ __device__ __forceinline__ const StepK<R> &step_consts(const Phys &ph)
@@ -239,6 +247,8 @@ inline StepK<R> make_step_consts(const Phys &ph)
     k.t0 = (R)ph.t0;
     k.thot = (R)ph.thot;
     k.tcold = (R)ph.tcold;
+    k.tla = (R)ph.tla;
+    k.tlb = (R)ph.tlb;
     return k;
 }
 
@@ -311,7 +321,7 @@ struct PGeo {
     int ic[3];
     float h[3], c[3];
     float rf2, band;
-    float v[3], w[3], T, momk, t0;   // velocity, spin, temperature; 2 rho0 / c_s^2; T_REF
+    float v[3], w[3], T, momk;       // velocity, spin, temperature; 2 rho0 / c_s^2
 };
 
 struct PartBuffers {

@@ -39,10 +39,13 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     const StepK<R> &K = step_consts<R>(ph);
 
     // Shifted-FP16 storage works in its scaled variables throughout: F_i = f_i / w_i and
-    // G_i = g_i / w_i - T0 are what the memory holds, the moments take the weights once per
-    // lattice-weight class, and the collision constants are divided by w_i (no per-population
-    // scaling on load or store).  The other modes work on f_i and g_i.
+    // G_i = g_i / w_i - T_c(x_home) are what the memory holds (T_c the conduction profile at the
+    // slot's home node), the moments take the weights once per lattice-weight class, and the
+    // collision constants are divided by w_i (no per-population scaling on load or store).  A
+    // pulled G_i is relative to s_i = T_c(x - c_ix) = Tc - tlb c_ix, a linear function of c_ix, so
+    // its moment and collision corrections are closed-form.  The other modes work on f_i and g_i.
     constexpr bool SC = MODE == RBTP_STORE_F16S;
+    const R Tc = SC ? K.tla + K.tlb * (R)ix : (R)0;   // T_c at this node
     // both populations of a slot (one access in the paired layouts of the float modes)
     auto ldfg = [&](const S *p, double w, R &fv, R &gv) {
         if constexpr (SC) {
@@ -81,6 +84,29 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
             }
         }
     });
+    if constexpr (!PULL && SC) {
+        // home slots (first step after a load): every G_i is relative to T_c(x), not s_i
+        unroll<27>([&](auto I) {
+            constexpr int i = decltype(I)::value;
+            constexpr int cx = dcx(i);
+            if constexpr (cx != 0) g[i] += K.tlb * (R)cx;
+        });
+    }
+    if constexpr (PULL && SC) {
+        // a bounce-back slot's home is this node: re-express its G relative to s_i (one branch
+        // around the whole correction, taken only by box-surface nodes)
+        if (xlo || xhi || ylo || yhi || zlo || zhi) {
+            unroll<27>([&](auto I) {
+                constexpr int i = decltype(I)::value;
+                constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+                if constexpr (i != 0 && cx != 0) {
+                    const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
+                                     (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
+                    if (out) g[i] += K.tlb * (R)cx;
+                }
+            });
+        }
+    }
     if constexpr (PULL) {
         // streaming.cu:45-61: at the x walls a direction that leaves only through x takes the
         // Dirichlet anti-bounce-back with the node's density deviation of the previous step; y/z
@@ -97,7 +123,8 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
                     if (ox && !oyz) {
                         if constexpr (SC) {
                             const R wi = (R)dweight(i);
-                            g[i] = wall_image(wi * (g[i] + K.t0), dweight(i), tw, rw) * (R)(1.0 / dweight(i)) - K.t0;
+                            const R si = Tc - K.tlb * (R)cx;
+                            g[i] = wall_image(wi * (g[i] + si), dweight(i), tw, rw) * (R)(1.0 / dweight(i)) - si;
                         } else {
                             g[i] = wall_image(g[i], dweight(i), tw, rw);
                         }
@@ -113,7 +140,8 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     if constexpr (SC) {
         // per weight class: sums of the scaled variables, then one multiply by the class weight
         rho = (R)dweight(0) * f[0];
-        phi = (R)dweight(0) * g[0] + K.t0;   // sum_i w_i (G_i + T0), sum_i w_i = 1
+        phi = (R)dweight(0) * g[0] + Tc;     // sum_i w_i (G_i + s_i), sum_i w_i s_i = T_c
+        kx = -K.tlb * (R)(1.0 / 3.0);        // sum_i c_i w_i s_i = -tlb sum_i w_i c_i c_ix
         unroll<3>([&](auto C) {
             constexpr int c = decltype(C)::value + 1;
             R r_ = 0, p_ = 0, ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
@@ -197,8 +225,9 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     const R pt = phi * K.tcinv;
     const R ptb = pt * ((R)1 + rho);
 
-    // scaled g: G* = g*/w - T0 = omc G + (g* - omc g)/w + (omc - 1) T0
-    const R gshift = SC ? (K.omc - (R)1) * K.t0 : (R)0;
+    // scaled g at home: G* = g*/w - T_c = omc G + (g* - omc g)/w + (omc - 1) T_c - omc tlb c_ix
+    const R gshift = SC ? (K.omc - (R)1) * Tc : (R)0;
+    const R gtilt = SC ? -K.omc * K.tlb : (R)0;
     {
         constexpr R w0 = (R)dweight(0);
         if constexpr (SC) {
@@ -241,7 +270,8 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
                     wD += (R)cx * (q * ce + cd);    // w cx G (1 + A)
                 }
                 const R gS = q * ga + gb;           // w pt (1 + rho + A)
-                const R gD = cu * gc + cV;          // w pt B + w c.V
+                R gD = cu * gc + cV;                // w pt B + w c.V
+                if constexpr (SC && cx != 0) gD += (R)cx * gtilt;
                 const R fi = f[i], fo = f[o], gi = g[i], go = g[o];
                 f[i] = K.om * fi + (wS + wD);
                 f[o] = K.om * fo + (wS - wD);
@@ -258,7 +288,7 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
             fout[(long long)i * L + node] = __floats2half2_rn(f[i], g[i]);
             if constexpr (OUT == OUT_MACROS_COL) {
                 b.fcol[(long long)i * L + node] = (double)((R)w * f[i]);
-                b.gcol[(long long)i * L + node] = (double)((R)w * (g[i] + K.t0));
+                b.gcol[(long long)i * L + node] = (double)((R)w * (g[i] + Tc));
             }
         } else {
             if constexpr (ST::PAIRED) {

@@ -90,8 +90,9 @@ def test_size_independent_properties_fullsize_fp64(env):
     assert np.all(np.isfinite(row))
 
 
-@pytest.mark.parametrize("storage,tol_phi,tol_u,tol_nu", [(STORE_F32, 5e-6, 1e-3, 1e-3),
-                                                          (STORE_F16S, 2e-3, 0.3, 5e-2)])
+# measured: FP32 phi 1.1e-6, ux 7e-6, Nu 5e-5; shifted FP16 phi 1.4e-6, ux 3.2e-4, Nu 7e-6
+@pytest.mark.parametrize("storage,tol_phi,tol_u,tol_nu", [(STORE_F32, 5e-6, 1e-4, 1e-3),
+                                                          (STORE_F16S, 2e-5, 3e-3, 1e-3)])
 def test_reduced_storage_against_fp64(env, storage, tol_phi, tol_u, tol_nu):
     cfg = W.config("plain_fp64", storage=storage)
     s = Solver(cfg)
@@ -99,8 +100,12 @@ def test_reduced_storage_against_fp64(env, storage, tol_phi, tol_u, tol_nu):
     f, g, f7 = W.initial_state(cfg)
     s.load_state(f, g, f7)
     o.load_state(f, g, f7)
-    s.step(100, macros_last=True)
-    o.step(100)
+    # the first step after a load collides home slots (no pull)
+    s.step(1, macros_last=True)
+    o.step(1)
+    assert rel_l2(s.macros()["phi"], o.macros()["phi"]) < 1e-6
+    s.step(99, macros_last=True)
+    o.step(99)
     ms, mo = s.macros(), o.macros()
     assert rel_l2(ms["phi"], mo["phi"]) < tol_phi
     assert rel_l2(ms["ux"], mo["ux"]) < tol_u
