@@ -470,14 +470,17 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const int o = dopp_rt(ip);
             const float wr = fweight_rt(ip), winv = finvweight_rt(ip);   // w_opp = w_ip
             // (f_i, g_i) slots of the paired layout
-            auto ldf = [&](const S *ptr) -> float {
-                if constexpr (MODE == RBTP_STORE_F16S) return __low2float(*ptr) * wr;
-                else return ptr->x;
-            };
-            // shifted-FP16 g holds g / w - T_c(x_home): the slot's home node x-index gives the shift
-            auto ldg = [&](const S *ptr, int ixh) -> float {
-                if constexpr (MODE == RBTP_STORE_F16S) return (__high2float(*ptr) + (tla + tlb * (float)ixh)) * wr;
-                else return ptr->y;
+            // both populations of a paired slot in one access; shifted-FP16 g holds
+            // g / w - T_c(x_home), the slot's home node x-index gives the shift
+            auto ld2 = [&](const S *ptr, int ixh, float &fv, float &gv) {
+                const S v = *ptr;
+                if constexpr (MODE == RBTP_STORE_F16S) {
+                    fv = __low2float(v) * wr;
+                    gv = (__high2float(v) + (tla + tlb * (float)ixh)) * wr;
+                } else {
+                    fv = v.x;
+                    gv = v.y;
+                }
             };
             // moving wall velocity at the intersection point (ibb.cu:33-46)
             const float relx = ((float)(ix - ipx) + hx) + q * (float)cxi;
@@ -495,30 +498,24 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const long long x1 = in1 ? ((long long)iz1 * geo.lxy + (long long)iy1 * geo.lx + ix1) : 0;
             const bool fluid1 = in1 && owner_cur[x1] < 0;
 
-            const float f_here = ldf(fB + (long long)ip * L + x);
-            const float g_here = ldg(gB + (long long)ip * L + x, ix);
+            float f_here, g_here;
+            ld2(fB + (long long)ip * L + x, ix, f_here, g_here);
+            // ibb.cu:52-73 (f: q < 0.5) and ibb.cu:114-128 (g: q <= 0.5) interpolate with the
+            // upstream slot (ip, x - c_ip) below q = 1/2 and with the opposite slot (opp, x) above
+            float f_up = 0.0f, g_up = 0.0f, f_oc = 0.0f, g_oc = 0.0f;
+            if (fluid1 && q <= 0.5f) ld2(fB + (long long)ip * L + x1, ix1, f_up, g_up);
+            if (fluid1 && q >= 0.5f) ld2(fB + (long long)o * L + x, ix, f_oc, g_oc);
             float fval, gval;
-            // ibb.cu:52-73 (f: q < 0.5), ibb.cu:114-128 (g: q <= 0.5)
             if (fluid1) {
-                if (q < 0.5f) {
-                    const float f_up = ldf(fB + (long long)ip * L + x1);
-                    fval = 2.0f * q * f_here + (1.0f - 2.0f * q) * f_up - mom;
-                } else {
-                    const float f_oc = ldf(fB + (long long)o * L + x);
-                    fval = (f_here - mom) * inv_2q + (2.0f * q - 1.0f) * inv_2q * f_oc;
-                }
+                if (q < 0.5f) fval = 2.0f * q * f_here + (1.0f - 2.0f * q) * f_up - mom;
+                else fval = (f_here - mom) * inv_2q + (2.0f * q - 1.0f) * inv_2q * f_oc;
             } else {
                 fval = f_here - mom;
             }
             const float amp = 2.0f * wr * Tpf * (1.0f + (float)rho[x]);
             if (fluid1) {
-                if (q <= 0.5f) {
-                    const float gu = ldg(gB + (long long)ip * L + x1, ix1);
-                    gval = -(2.0f * q * g_here + (1.0f - 2.0f * q) * gu) + amp;
-                } else {
-                    const float go = ldg(gB + (long long)o * L + x, ix);
-                    gval = -g_here * inv_2q + amp * inv_2q + (2.0f * q - 1.0f) * inv_2q * go;
-                }
+                if (q <= 0.5f) gval = -(2.0f * q * g_here + (1.0f - 2.0f * q) * g_up) + amp;
+                else gval = -g_here * inv_2q + amp * inv_2q + (2.0f * q - 1.0f) * inv_2q * g_oc;
             } else {
                 gval = -g_here + amp;
             }
@@ -532,8 +529,7 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
                 // the value the reference would read back is the rounded one
                 const int ixs = ix + cxi;   // home of the written slot: the solid node
                 *fs = __floats2half2_rn(fval * winv, gval * winv - (tla + tlb * (float)ixs));
-                f_out = ldf(fs);
-                g_out = ldg(fs, ixs);
+                ld2(fs, ixs, f_out, g_out);
             } else {
                 *fs = make_float2(fval, gval);
             }
