@@ -433,9 +433,14 @@ int run(int argc, char **argv)
         for (int s = 0; s < steps; ++s) step();
         CU(cuCtxSynchronize());
         const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        // state check: non-finite temperatures after the run
+        std::vector<double> phi(L);
+        CU(cuMemcpyDtoH(phi.data(), d_phi, L * sizeof(double)));
+        long long bad = 0;
+        for (long long n = 0; n < L; ++n) bad += std::isfinite(phi[n]) ? 0 : 1;
         std::printf("ref_time ms_per_step %.6f ms_per_step_with_host_scans %.6f steps %d warmup %d nodes %lld "
-                    "npart %d links %d\n", 1e3 * (sec - g_scan_seconds) / steps, 1e3 * sec / steps, steps, warm,
-                    L, NP, num_links);
+                    "npart %d links %d nonfinite %lld\n", 1e3 * (sec - g_scan_seconds) / steps, 1e3 * sec / steps,
+                    steps, warm, L, NP, num_links, bad);
         CU(cuModuleUnload(mod));
         CU(cuDevicePrimaryCtxRelease(dev));
         return 0;

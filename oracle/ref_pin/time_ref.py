@@ -93,6 +93,7 @@ def main() -> int:
         "steps": int(kv["steps"]), "warmup": int(kv["warmup"]), "ms_per_step": ms,
         "ms_per_step_with_host_scans": float(kv["ms_per_step_with_host_scans"]),
         "mlups": int(kv["nodes"]) / (ms * 1e-3) / 1e6,
+        "nonfinite_phi_nodes_after_run": int(kv["nonfinite"]),
         "what": "reference kernels (its sources, nvcc -O3 sm_103a, FP64) in its host-loop order incl. D2D copies",
     }))
     return 0

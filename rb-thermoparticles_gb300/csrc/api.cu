@@ -217,7 +217,7 @@ int rbtp_footprint(const rbtp_config *cfg, size_t *bytes)
         const size_t lcap = (size_t)std::min<long long>(26 * shell_bound(r, r + std::sqrt(3.0)), 1LL << 30);
         b += (size_t)np * lcap * (2 * sizeof(int) + sizeof(double)) + np * sizeof(int);
         const long long nf_bound = (long long)np * shell_bound(r, r + 1.7606816861659007);
-        const size_t nfc = (size_t)std::min<long long>(nf_bound, std::max<long long>(8192, (long long)np * 128));
+        const size_t nfc = (size_t)std::min<long long>(nf_bound, 1LL << 28);
         b += nfc * (2 * sizeof(int) + 59 * sizeof(double));
         const double cs = 2.0 * r + std::max(cfg->rep_min_gap, 0.0) + 1e-9;
         size_t nc = 1;
@@ -327,7 +327,10 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
         const long long nf_bound = (long long)np * shell_bound(r, r + 1.7606816861659007);
         // a sphere uncovers a few nodes per step; 128 per sphere per step (or the shell bound) is
         // far beyond any stable LBM velocity, and an overflow is reported, not written past
-        pb.nf_cap = (int)std::min<long long>(nf_bound, std::max<long long>(8192, (long long)np * 128));
+        // the proven bound (every node within 1.76 of a sphere's surface becoming fluid at once):
+        // fast spheres (the reference's density ratio 1.5 at LX = 320 reaches several lattice
+        // units per step) refill hundreds of nodes per sphere and step
+        pb.nf_cap = (int)std::min<long long>(nf_bound, 1LL << 28);
         CKC(dalloc(&pb.nf_node, (size_t)pb.nf_cap)); CKC(dalloc(&pb.nf_pid, (size_t)pb.nf_cap));
         CKC(dalloc(&pb.nf_val, (size_t)pb.nf_cap * 54)); CKC(dalloc(&pb.nf_mac, (size_t)pb.nf_cap * 5));
         // contact cell list: cells no narrower than the interaction range 2r + REP_MIN_GAP

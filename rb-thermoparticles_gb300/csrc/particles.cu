@@ -644,7 +644,7 @@ __global__ void k_cell_fill(const PartBuffers pb)
     if (p < pb.np) cell_fill_body(pb, p);
 }
 
-constexpr int MAX_CAND = 64;
+constexpr int MAX_CAND = 256;   // contact partners of one sphere (33 fit without overlap at r = 8)
 // Per-particle CTAs (marking, link fill, new-fluid detection) are LINK_WIDE threads while fewer
 // particles than this are in flight (4 CTAs per SM of a 152-SM GB300) and LINK_NARROW beyond; the
 // results do not depend on the width.
