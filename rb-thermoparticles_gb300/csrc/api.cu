@@ -665,7 +665,7 @@ int rbtp_get_links(rbtp_handle *h, int *n, int *node, int *dir, int *pid, double
         CK(cudaMemcpy(hn.data(), h->pb.link_node + p * slab, c * sizeof(int), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(hd.data(), h->pb.link_dir + p * slab, c * sizeof(int), cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(hq.data(), h->pb.link_q + p * slab, c * sizeof(double), cudaMemcpyDeviceToHost));
-        for (int k = 0; k < c; ++k) all.push_back({hn[k], hd[k], p, hq[k]});
+        for (int k = 0; k < c; ++k) all.push_back({hn[k], hd[k] & LINK_DIR_MASK, p, hq[k]});
     }
     std::sort(all.begin(), all.end(), [](const Lk &a, const Lk &b) {
         return a.node != b.node ? a.node < b.node : a.dir < b.dir;

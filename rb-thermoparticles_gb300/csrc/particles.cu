@@ -351,8 +351,8 @@ constexpr int IBB_THREADS = 128;
 
 template <int MODE>
 __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                                               const int *owner_cur, void *f_, void *g_,
-                                               const double *rho, int p, int chunk, double *sh)
+                                               void *f_, void *g_, const double *rho, int p, int chunk,
+                                               double *sh)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
@@ -371,7 +371,8 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
     if constexpr (MODE == RBTP_STORE_F64) {
         for (int t = chunk * IBB_THREADS + threadIdx.x; t < n; t += pb.ibb_chunks * IBB_THREADS) {
             const int x = pb.link_node[base + t];
-            const int ip = pb.link_dir[base + t];
+            const int dw = pb.link_dir[base + t];
+            const int ip = dw & LINK_DIR_MASK;
             const double q = pb.link_q[base + t];
             const int iz = x / (int)geo.lxy;
             const int rem = x - iz * (int)geo.lxy;
@@ -391,10 +392,9 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const double mom = 2.0 * w * ph.rho0 * evel * 3.0;
             const double inv_2q = (q >= 0.5) ? 0.5 / q : 0.0;
 
-            const int ix1 = ix - cxi, iy1 = iy - cyi, iz1 = iz - czi;
-            const bool in1 = ix1 >= 0 && ix1 < geo.lx && iy1 >= 0 && iy1 < geo.ly && iz1 >= 0 && iz1 < geo.lz;
-            const long long x1 = in1 ? ((long long)iz1 * geo.lxy + (long long)iy1 * geo.lx + ix1) : 0;
-            const bool fluid1 = in1 && owner_cur[x1] < 0;
+            // upstream node x - c_ip, in-domain fluid (flag from the link build's owner reads)
+            const bool fluid1 = (dw >> LINK_UP) & 1;
+            const long long x1 = (long long)x - cxi - (long long)cyi * geo.lx - (long long)czi * geo.lxy;
 
             const double f_here = fB[(long long)ip * L + x];
             const double g_here = gB[(long long)ip * L + x];
@@ -458,10 +458,62 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
 #pragma unroll
         for (int k = 0; k < 7; ++k) sum[k] = df{0.0f, 0.0f};
         auto add = [&](int k, float v) { sum[k] = df_add(sum[k], df{v, 0.0f}); };
-        for (int t = chunk * IBB_THREADS + threadIdx.x; t < n; t += pb.ibb_chunks * IBB_THREADS) {
-            const int x = pb.link_node[base + t];
-            const int ip = pb.link_dir[base + t];
-            const float q = (float)pb.link_q[base + t];
+        // (f_i, g_i) slots of the paired layout: both populations of a slot in one access;
+        // shifted-FP16 g holds g / w - T_c(x_home), the slot's home node x-index gives the shift
+        auto ld2 = [&](const S *ptr, int ixh, float wr, float &fv, float &gv) {
+            const S v = *ptr;
+            if constexpr (MODE == RBTP_STORE_F16S) {
+                fv = __low2float(v) * wr;
+                gv = (__high2float(v) + (tla + tlb * (float)ixh)) * wr;
+            } else {
+                fv = v.x;
+                gv = v.y;
+            }
+        };
+        // Gathered inputs of one link.  A link reads slots of fluid nodes only (x and, when it
+        // interpolates, x - c_ip) and writes the slot of a solid node (x + c_ip), so the gathers of
+        // later links may be issued before the stores of earlier ones: two links are gathered per
+        // iteration to keep twice the loads in flight.  Each thread still sums its links in
+        // ascending order.
+        struct LinkIn {
+            int x, ip;
+            float q, f_here, g_here, f_2, g_2, rho;
+            bool fluid1;
+        };
+        auto gather = [&](int t, LinkIn &a) {
+            a.x = pb.link_node[base + t];
+            const int dw = pb.link_dir[base + t];
+            a.ip = dw & LINK_DIR_MASK;
+            a.q = (float)pb.link_q[base + t];
+            a.fluid1 = (dw >> LINK_UP) & 1;   // upstream node x - c_ip is in-domain fluid
+            const int ip = a.ip, x = a.x;
+            const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
+            const float wr = fweight_rt(ip);
+            const int ix = x % geo.lx;
+            ld2(fB + (long long)ip * L + x, ix, wr, a.f_here, a.g_here);
+            // ibb.cu:52-73 (f: q < 0.5) and ibb.cu:114-128 (g: q <= 0.5) interpolate with the
+            // upstream slot (ip, x - c_ip) below q = 1/2 and with the opposite slot (opp, x) above;
+            // at q = 1/2 f takes the opposite slot and g the upstream one (both are loaded)
+            a.f_2 = a.g_2 = 0.0f;
+            if (a.fluid1) {
+                float fu, gu, fo, go;
+                if (a.q <= 0.5f) {
+                    const long long x1 = (long long)x - cxi - (long long)cyi * geo.lx - (long long)czi * geo.lxy;
+                    ld2(fB + (long long)ip * L + x1, ix - cxi, wr, fu, gu);
+                    a.f_2 = fu;
+                    a.g_2 = gu;
+                }
+                if (a.q >= 0.5f) {
+                    ld2(fB + (long long)dopp_rt(ip) * L + x, ix, wr, fo, go);
+                    a.f_2 = fo;
+                    if (a.q > 0.5f) a.g_2 = go;
+                }
+            }
+            a.rho = (float)rho[x];
+        };
+        auto finish = [&](const LinkIn &a) {
+            const int x = a.x, ip = a.ip;
+            const float q = a.q, f_here = a.f_here, g_here = a.g_here;
             const int iz = x / (int)geo.lxy;
             const int rem = x - iz * (int)geo.lxy;
             const int iy = rem / geo.lx;
@@ -469,19 +521,6 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
             const int o = dopp_rt(ip);
             const float wr = fweight_rt(ip), winv = finvweight_rt(ip);   // w_opp = w_ip
-            // (f_i, g_i) slots of the paired layout
-            // both populations of a paired slot in one access; shifted-FP16 g holds
-            // g / w - T_c(x_home), the slot's home node x-index gives the shift
-            auto ld2 = [&](const S *ptr, int ixh, float &fv, float &gv) {
-                const S v = *ptr;
-                if constexpr (MODE == RBTP_STORE_F16S) {
-                    fv = __low2float(v) * wr;
-                    gv = (__high2float(v) + (tla + tlb * (float)ixh)) * wr;
-                } else {
-                    fv = v.x;
-                    gv = v.y;
-                }
-            };
             // moving wall velocity at the intersection point (ibb.cu:33-46)
             const float relx = ((float)(ix - ipx) + hx) + q * (float)cxi;
             const float rely = ((float)(iy - ipy) + hy) + q * (float)cyi;
@@ -492,30 +531,17 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const float evel = (float)cxi * uwx + (float)cyi * uwy + (float)czi * uwz;
             const float mom = wr * mom_k * evel;
             const float inv_2q = (q >= 0.5f) ? 0.5f / q : 0.0f;
-
-            const int ix1 = ix - cxi, iy1 = iy - cyi, iz1 = iz - czi;
-            const bool in1 = ix1 >= 0 && ix1 < geo.lx && iy1 >= 0 && iy1 < geo.ly && iz1 >= 0 && iz1 < geo.lz;
-            const long long x1 = in1 ? ((long long)iz1 * geo.lxy + (long long)iy1 * geo.lx + ix1) : 0;
-            const bool fluid1 = in1 && owner_cur[x1] < 0;
-
-            float f_here, g_here;
-            ld2(fB + (long long)ip * L + x, ix, f_here, g_here);
-            // ibb.cu:52-73 (f: q < 0.5) and ibb.cu:114-128 (g: q <= 0.5) interpolate with the
-            // upstream slot (ip, x - c_ip) below q = 1/2 and with the opposite slot (opp, x) above
-            float f_up = 0.0f, g_up = 0.0f, f_oc = 0.0f, g_oc = 0.0f;
-            if (fluid1 && q <= 0.5f) ld2(fB + (long long)ip * L + x1, ix1, f_up, g_up);
-            if (fluid1 && q >= 0.5f) ld2(fB + (long long)o * L + x, ix, f_oc, g_oc);
             float fval, gval;
-            if (fluid1) {
-                if (q < 0.5f) fval = 2.0f * q * f_here + (1.0f - 2.0f * q) * f_up - mom;
-                else fval = (f_here - mom) * inv_2q + (2.0f * q - 1.0f) * inv_2q * f_oc;
+            if (a.fluid1) {
+                if (q < 0.5f) fval = 2.0f * q * f_here + (1.0f - 2.0f * q) * a.f_2 - mom;
+                else fval = (f_here - mom) * inv_2q + (2.0f * q - 1.0f) * inv_2q * a.f_2;
             } else {
                 fval = f_here - mom;
             }
-            const float amp = 2.0f * wr * Tpf * (1.0f + (float)rho[x]);
-            if (fluid1) {
-                if (q <= 0.5f) gval = -(2.0f * q * g_here + (1.0f - 2.0f * q) * g_up) + amp;
-                else gval = -g_here * inv_2q + amp * inv_2q + (2.0f * q - 1.0f) * inv_2q * g_oc;
+            const float amp = 2.0f * wr * Tpf * (1.0f + a.rho);
+            if (a.fluid1) {
+                if (q <= 0.5f) gval = -(2.0f * q * g_here + (1.0f - 2.0f * q) * a.g_2) + amp;
+                else gval = -g_here * inv_2q + amp * inv_2q + (2.0f * q - 1.0f) * inv_2q * a.g_2;
             } else {
                 gval = -g_here + amp;
             }
@@ -528,8 +554,10 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             if constexpr (MODE == RBTP_STORE_F16S) {
                 // the value the reference would read back is the rounded one
                 const int ixs = ix + cxi;   // home of the written slot: the solid node
-                *fs = __floats2half2_rn(fval * winv, gval * winv - (tla + tlb * (float)ixs));
-                ld2(fs, ixs, f_out, g_out);
+                const __half2 hv = __floats2half2_rn(fval * winv, gval * winv - (tla + tlb * (float)ixs));
+                *fs = hv;
+                f_out = __low2float(hv) * wr;
+                g_out = (__high2float(hv) + (tla + tlb * (float)ixs)) * wr;
             } else {
                 *fs = make_float2(fval, gval);
             }
@@ -544,6 +572,20 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             add(4, relz * Fx - relx * Fz);
             add(5, relx * Fy - rely * Fx);
             add(6, g_here - g_out);
+        };
+        const int stride = pb.ibb_chunks * IBB_THREADS;
+        int t = chunk * IBB_THREADS + threadIdx.x;
+        for (; t + stride < n; t += 2 * stride) {
+            LinkIn a, b;
+            gather(t, a);
+            gather(t + stride, b);
+            finish(a);
+            finish(b);
+        }
+        if (t < n) {
+            LinkIn a;
+            gather(t, a);
+            finish(a);
         }
         // double-float block sum (FP32 pipe), one FP64 value per quantity
         block_reduce_df<7, IBB_THREADS>(sum, acc, reinterpret_cast<float *>(sh));
@@ -568,7 +610,7 @@ __global__ void __launch_bounds__(IBB_THREADS, MODE == RBTP_STORE_F64 ? 4 : 6) k
                                                            void *g_, const double *rho)
 {
     __shared__ double sh[7 * IBB_THREADS];
-    links_ibb_body<MODE>(geo, ph, pb, pb.owner_cur, f_, g_, rho, blockIdx.x, blockIdx.y, sh);
+    links_ibb_body<MODE>(geo, ph, pb, f_, g_, rho, blockIdx.x, blockIdx.y, sh);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -871,29 +913,31 @@ __global__ void __launch_bounds__(NT) k_mark(const Geo geo, const Phys ph, const
 
 // ------------------------------------------------------------------------------------------------
 // Link slabs (links.cu:50-139): CTA per particle, ordered compaction over its padded box.
-// Phase 1 (integer work only): every fluid node of the box within r + 2 of the centre marks the
-// directions whose neighbour this particle owns (a 27-bit mask per node); an exclusive scan of the
-// mask popcounts numbers the candidates (node, direction) in node-then-direction order.  Phase 2:
-// candidate k is located by a binary search over the scan and a bit select in its node's mask, the
-// ray-sphere q of links.cu:7-23 runs with all lanes busy, and accepted links are appended to the
-// particle's slab in the same order.  Only the spherical shell that can hold link nodes is
+// Phase 1 (integer work only): every fluid node of the box within r + 2 of the centre reads the
+// owners of its 26 neighbours and marks the directions whose neighbour this particle owns (a 27-bit
+// mask per node); an exclusive scan of the mask popcounts numbers the candidates (node, direction)
+// in node-then-direction order.  Phase 2: candidate k is located by a binary search over the scan
+// and a bit select in its node's mask, the ray-sphere q of links.cu:7-23 runs with all lanes busy,
+// and accepted links are appended to the particle's slab in the same order (the reference's
+// (idx, ip) order, links.cu:221-250).  Only the spherical shell that can hold link nodes is
 // enumerated: per (y, z) row of the box, the x-intervals between an inner radius (nodes inside it
 // are certainly solid) and the outer reach r + 2, with float margins so that every possible link
 // node is kept; rows are numbered by a block scan and flat indices are mapped back by a binary
-// search, so nodes are still visited in ascending index order (the link order is unchanged).
+// search, so nodes are visited in ascending index order.  The same owner reads give, per link,
+// whether the upstream node x - c_ip is an in-domain fluid node (the interpolating branch of
+// ibb.cu:52-73 / 114-128); it is stored in bit LINK_UP of the direction word so that the IBB pass
+// needs no flag gather.
 // ------------------------------------------------------------------------------------------------
 // CTA size: 512 threads when few particles are in flight (the per-particle chain is the latency),
 // 128 when many are (more particles per SM); the links are identical either way.
 constexpr int LINK_WIDE = 512, LINK_NARROW = 128;
-// (y, z) rows of the shell table (larger boxes scan the whole box)
-template <int NT> constexpr int link_max_rows() { return NT >= 512 ? 2048 : 1024; }
-
 
 // Shared scratch of one link-fill CTA.
 template <int NT>
 struct LinkShared {
     ShellRows<NT> rows;       // shell table (its wsum also serves the chunk scans)
     unsigned mask[NT];        // candidate directions of each chunk node (bit ip)
+    unsigned up[NT];          // directions whose neighbour is in-domain fluid (bit ip)
     int scan[NT];             // exclusive prefix of the popcounts
     int node[NT];             // lattice index of each chunk node
 };
@@ -902,7 +946,6 @@ template <bool F32Q, int NT>
 __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
                                                const int *owner, DevStatus *status, int p, LinkShared<NT> &sm)
 {
-    constexpr int LINK_THREADS = NT;
     const PGeo &pg = pb.pgeo[p];
     const float r = (float)ph.radius;
     const Box b = pgeo_box(pg.lbox);
@@ -919,14 +962,15 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
     // exact node-centre offsets for the float q: integer part of the centre and its fraction
     const int ipx = pg.ic[0], ipy = pg.ic[1], ipz = pg.ic[2];
     const float hx = pg.h[0], hy = pg.h[1], hz = pg.h[2];
+    const int lx = geo.lx, lxy = (int)geo.lxy;
     // shell |x - X| in [r_in, r_out]: nodes closer than r_in are inside the sphere (solid)
     int total = shell_rows_build<NT>(sm.rows, b, pxf, pyf, pzf, fmaxf(r - 0.05f, 0.0f), reach + 0.01f);
     const bool use_rows = total >= 0;
     if (!use_rows) total = nx * ny * nz;
     int base = 0;
-    for (int c0 = 0; c0 < total; c0 += LINK_THREADS) {
+    for (int c0 = 0; c0 < total; c0 += NT) {
         const int t = c0 + threadIdx.x;
-        unsigned mask = 0;
+        unsigned mask = 0, up = 0;
         int my_node = 0;
         if (t < total) {
             int ix, iy, iz;
@@ -943,45 +987,57 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
             const float ddx = ((float)ix + 0.5f) - pxf, ddy = ((float)iy + 0.5f) - pyf,
                         ddz = ((float)iz + 0.5f) - pzf;
             const long long idx = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
-            if (ddx * ddx + ddy * ddy + ddz * ddz <= reach2 && owner[idx] < 0) {
-                unroll<26>([&](auto K) {
-                    constexpr int ip = decltype(K)::value + 1;
-                    constexpr int cx = dcx(ip), cy = dcy(ip), cz = dcz(ip);
-                    const int xn = ix + cx, yn = iy + cy, zn = iz + cz;
-                    if (xn >= 0 && xn < geo.lx && yn >= 0 && yn < geo.ly && zn >= 0 && zn < geo.lz) {
-                        const long long nidx = idx + cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
-                        if (owner[nidx] == p) mask |= 1u << ip;
-                    }
-                });
+            const int *on = owner + idx;
+            if (ddx * ddx + ddy * ddy + ddz * ddz <= reach2 && __ldg(on) < 0) {
+                if (ix > 0 && ix < geo.lx - 1 && iy > 0 && iy < geo.ly - 1 && iz > 0 && iz < geo.lz - 1) {
+                    // interior node: all 26 neighbours are in the domain
+                    unroll<26>([&](auto K) {
+                        constexpr int ip = decltype(K)::value + 1;
+                        const int o = __ldg(on + (dcx(ip) + dcy(ip) * lx + dcz(ip) * lxy));
+                        if (o == p) mask |= 1u << ip;
+                        if (o < 0) up |= 1u << ip;
+                    });
+                } else {
+                    unroll<26>([&](auto K) {
+                        constexpr int ip = decltype(K)::value + 1;
+                        constexpr int cx = dcx(ip), cy = dcy(ip), cz = dcz(ip);
+                        const int xn = ix + cx, yn = iy + cy, zn = iz + cz;
+                        if (xn >= 0 && xn < geo.lx && yn >= 0 && yn < geo.ly && zn >= 0 && zn < geo.lz) {
+                            const int o = __ldg(on + (cx + cy * lx + cz * lxy));
+                            if (o == p) mask |= 1u << ip;
+                            if (o < 0) up |= 1u << ip;
+                        }
+                    });
+                }
             }
             my_node = (int)idx;
         }
         int ccount;
         const int pos = block_exclusive_scan<NT>(__popc(mask), sm.rows.wsum, ccount);
         sm.mask[threadIdx.x] = mask;
+        sm.up[threadIdx.x] = up;
         sm.scan[threadIdx.x] = pos;
         sm.node[threadIdx.x] = my_node;
         __syncthreads();
         // phase 2: q for the numbered candidates, order-preserving append
-        for (int k0 = 0; k0 < ccount; k0 += LINK_THREADS) {
+        for (int k0 = 0; k0 < ccount; k0 += NT) {
             const int k = k0 + threadIdx.x;
-            int ok = 0, node = 0, ip = 0;
+            int ok = 0, node = 0, dw = 0;
             double q = 0.0;
             if (k < ccount) {
                 // the chunk thread j holding candidate k: the last j with scan[j] <= k
-                int lo = 0, hi = LINK_THREADS - 1;
+                int lo = 0, hi = NT - 1;
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
                     if (sm.scan[mid] <= k) lo = mid;
                     else hi = mid - 1;
                 }
-                unsigned m = sm.mask[lo];
-                for (int r = k - sm.scan[lo]; r > 0; --r) m &= m - 1;
-                ip = __ffs(m) - 1;
+                const int ip = (int)__fns(sm.mask[lo], 0u, k - sm.scan[lo] + 1);
                 node = sm.node[lo];
-                const int iz = node / (int)geo.lxy;
-                const int iy = (node - iz * (int)geo.lxy) / geo.lx;
-                const int ix = node - iz * (int)geo.lxy - iy * geo.lx;
+                dw = ip | (int)(((sm.up[lo] >> dopp_rt(ip)) & 1u) << LINK_UP);
+                const int iz = node / lxy;
+                const int iy = (node - iz * lxy) / lx;
+                const int ix = node - iz * lxy - iy * lx;
                 int r32 = -1;
                 if constexpr (F32Q)
                     r32 = link_q_f32(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (float)(ix - ipx) + hx,
@@ -1000,7 +1056,7 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
             if (ok) {
                 if (lpos < pb.link_cap) {
                     pb.link_node[slab + lpos] = node;
-                    pb.link_dir[slab + lpos] = ip;
+                    pb.link_dir[slab + lpos] = dw;
                     pb.link_q[slab + lpos] = q;
                 } else {
                     atomicOr(&status->link_overflow, 1);
@@ -1362,7 +1418,7 @@ __global__ void __launch_bounds__(IBB_THREADS, MODE == RBTP_STORE_F64 ? 4 : 6) k
     const CavDesc &d = desc[mp.x];
     if (d.out == OUT_IDLE) return;
     const int w = d.cur ^ 1;
-    links_ibb_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f[w], d.g[w], d.rho, mp.y, cm.y, sh);
+    links_ibb_body<MODE>(d.geo, d.ph, d.pb, d.f[w], d.g[w], d.rho, mp.y, cm.y, sh);
 }
 
 __global__ void k_cells_zero_b(const CavDesc *desc, const int *pmem)

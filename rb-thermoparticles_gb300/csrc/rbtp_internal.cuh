@@ -305,6 +305,9 @@ cudaError_t launch_forcing(const Geo &geo, const Phys &ph, const double *phi, do
 // chunk partial sums are added in chunk order by the integrator (deterministic, and the same in
 // single-cavity and batched runs).
 constexpr int IBB_CHUNKS = 8;
+// Bit of a link's direction word that marks an in-domain fluid upstream node x - c_ip (the
+// interpolating branch of the IBB); the direction is the word's low five bits.
+constexpr int LINK_UP = 5, LINK_DIR_MASK = 31;
 constexpr int ibb_chunks_for(long long link_cap)
 {
     return link_cap <= 2048 ? 1 : (link_cap >= 2048LL * IBB_CHUNKS ? IBB_CHUNKS : (int)((link_cap + 2047) / 2048));
@@ -333,7 +336,8 @@ struct PartBuffers {
     double *cF;             // contact force (3*np)
     int *owner_cur, *owner_new;   // solid owner maps (L each); -1 = fluid
     int link_cap;           // links per particle slab
-    int *link_node, *link_dir, *link_cnt;
+    int *link_node, *link_cnt;
+    int *link_dir;          // direction ip in bits 0-4, LINK_UP set when x - c_ip is in-domain fluid
     double *link_q;
     int nf_cap;
     int *nf_node, *nf_pid;
