@@ -59,9 +59,9 @@ template <int MODE, bool PULL>
 __device__ __forceinline__ void step_out(const CavDesc &d, const StepBuffers &b, int out, int ix, int iy,
                                          int iz)
 {
-    if (out == OUT_NONE) step_node<MODE, PULL, OUT_NONE>(d.geo, d.ph, b, ix, iy, iz);
-    else if (out == OUT_RHO) step_node<MODE, PULL, OUT_RHO>(d.geo, d.ph, b, ix, iy, iz);
-    else step_node<MODE, PULL, OUT_MACROS>(d.geo, d.ph, b, ix, iy, iz);
+    if (out == OUT_NONE) step_node<MODE, PULL, OUT_NONE, false>(d.geo, d.ph, b, ix, iy, iz);
+    else if (out == OUT_RHO) step_node<MODE, PULL, OUT_RHO, false>(d.geo, d.ph, b, ix, iy, iz);
+    else step_node<MODE, PULL, OUT_MACROS, false>(d.geo, d.ph, b, ix, iy, iz);
 }
 
 // The batched kernel carries all phase/output variants of the step body behind block-uniform

@@ -3,6 +3,8 @@
 // (many cavities over a packed tile table), which instantiate it for their launch shapes.
 #pragma once
 
+#include <type_traits>
+
 #include "rbtp_internal.cuh"
 
 // Resident 128-thread blocks per SM requested from the register allocator (FP64 is bound by the
@@ -17,8 +19,12 @@
 namespace rbtp {
 
 // One node of the fused step; shared by the single-cavity kernel below and the batched kernel of
-// batch.cu.  (ix, iy, iz) must lie inside the lattice.
-template <int MODE, bool PULL, int OUT>
+// batch.cu.  (ix, iy, iz) must lie inside the lattice.  INTERIOR_PATH adds a second copy of the
+// gather without the box-face tests, taken by warps none of whose nodes touches a face.  It pays
+// only where the step is issue-bound (shifted-FP16 storage: -11 % instructions, -11 % time at
+// 320x320x160); FP32 is HBM-bound and FP64 FP64-pipe-bound, and the batched kernel (six step
+// variants in one kernel, small cavities whose warps nearly all touch an x face) leaves it out.
+template <int MODE, bool PULL, int OUT, bool INTERIOR_PATH = true>
 __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const StepBuffers &b, int ix,
                                           int iy, int iz)
 {
@@ -59,31 +65,46 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
         }
     };
     R f[27], g[27];
-    unroll<27>([&](auto I) {
-        constexpr int i = decltype(I)::value;
-        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i), o = dopp(i);
-        constexpr double w = dweight(i);
-        if constexpr (!PULL || i == 0) {
-            if constexpr (ST::PAIRED) {
-                ldfg(fin + (long long)i * L + node, w, f[i], g[i]);
+    // INTERIOR: no neighbour of this warp's nodes leaves the box, so every pull is the plain
+    // f*_i(x - c_i) (the face tests and the bounce-back selects drop out)
+    auto gather = [&](auto INT) {
+        constexpr bool INTERIOR = decltype(INT)::value;
+        unroll<27>([&](auto I) {
+            constexpr int i = decltype(I)::value;
+            constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i), o = dopp(i);
+            constexpr double w = dweight(i);
+            if constexpr (!PULL || i == 0) {
+                if constexpr (ST::PAIRED) {
+                    ldfg(fin + (long long)i * L + node, w, f[i], g[i]);
+                } else {
+                    f[i] = ST::ld_f(fin + (long long)i * L + node, w, t0);
+                    g[i] = ST::ld_g(gin + (long long)i * L + node, w, t0);
+                }
             } else {
-                f[i] = ST::ld_f(fin + (long long)i * L + node, w, t0);
-                g[i] = ST::ld_g(gin + (long long)i * L + node, w, t0);
+                // f_i(x) = f*_i(x - c_i); a neighbour outside the box returns f*_opp(x) (bounce-back)
+                const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
+                long long src = (long long)i * L + node - off;
+                if constexpr (!INTERIOR) {
+                    const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
+                                     (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
+                    if constexpr (SC) {
+                        if (out) src = (long long)o * L + node;
+                    } else {
+                        src = out ? ((long long)o * L + node) : src;
+                    }
+                }
+                if constexpr (ST::PAIRED) {
+                    ldfg(fin + src, w, f[i], g[i]);
+                } else {
+                    f[i] = ST::ld_f(fin + src, w, t0);
+                    g[i] = ST::ld_g(gin + src, w, t0);
+                }
             }
-        } else {
-            // f_i(x) = f*_i(x - c_i); a neighbour outside the box returns f*_opp(x) (bounce-back)
-            const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
-                             (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
-            const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
-            const long long src = out ? ((long long)o * L + node) : ((long long)i * L + node - off);
-            if constexpr (ST::PAIRED) {
-                ldfg(fin + src, w, f[i], g[i]);
-            } else {
-                f[i] = ST::ld_f(fin + src, w, t0);
-                g[i] = ST::ld_g(gin + src, w, t0);
-            }
-        }
-    });
+        });
+    };
+    const bool face = xlo || xhi || ylo || yhi || zlo || zhi;
+    if (INTERIOR_PATH && SC && PULL && !__any_sync(__activemask(), face)) gather(std::true_type{});
+    else gather(std::false_type{});
     if constexpr (!PULL && SC) {
         // home slots (first step after a load): every G_i is relative to T_c(x), not s_i
         unroll<27>([&](auto I) {
