@@ -276,6 +276,11 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
     } while (0)
 
     CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    {
+        CKC(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        CKC(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+        CKC(cudaEventCreateWithFlags(&h->ev_contacts, cudaEventDisableTiming));
+    }
     const size_t sb = store_bytes(h->mode);
     const size_t P = (size_t)27 * (size_t)L;
     for (int k = 0; k < 2; ++k) {
@@ -357,6 +362,7 @@ int rbtp_destroy(rbtp_handle *h)
 {
     if (!h) return RBTP_OK;
     rbtp_batch_detach(h);
+    if (h->side) cudaStreamSynchronize(h->side);
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (int k = 0; k < 2; ++k) {
         if (h->g[k] != h->f[k]) cudaFree(h->g[k]);
@@ -374,6 +380,9 @@ int rbtp_destroy(rbtp_handle *h)
     cudaFree(pb.nf_node); cudaFree(pb.nf_pid); cudaFree(pb.nf_val); cudaFree(pb.nf_mac);
     cudaFree(pb.cell_count); cudaFree(pb.cell_start); cudaFree(pb.cell_fill); cudaFree(pb.cell_items);
     cudaFree(pb.pair_p); cudaFree(pb.pair_q);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_contacts) cudaEventDestroy(h->ev_contacts);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return RBTP_OK;
@@ -541,10 +550,18 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
         b.fcol = h->fcol; b.gcol = h->gcol; b.status = h->status;
         CK(launch_step(h->mode, h->phase == PHASE_COLLIDED, out, h->geo, h->ph, b, h->stream));
         if (parts) {
+            // Stream order: the contacts (positions only) run on the side stream beside IBB (both
+            // latency-bound, few CTAs); the integrator waits for the contact forces.  The link
+            // slabs stay on the main stream: beside the HBM-bound bulk kernel their CTAs would take
+            // its SM slots (measured slower).
             int *oc = h->owner[h->ocur], *on = h->owner[1 - h->ocur];
             h->pb.owner_cur = oc;
+            CK(cudaEventRecord(h->ev_fork, h->stream));
+            CK(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
+            CK(launch_contacts(h->geo, h->ph, h->pb, h->status, h->side));
+            CK(cudaEventRecord(h->ev_contacts, h->side));
             CK(launch_links_ibb(h->mode, h->geo, h->ph, h->pb, h->f[dst], h->g[dst], h->rho, h->stream));
-            CK(launch_contacts(h->geo, h->ph, h->pb, h->status, h->stream));
+            CK(cudaStreamWaitEvent(h->stream, h->ev_contacts, 0));
             CK(launch_update(h->ph, h->pb, h->stream));
             s = build_links(h, on);
             if (s) return s;

@@ -29,6 +29,9 @@ struct rbtp_handle {
     int mode = RBTP_STORE_F64;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // particle steps: side stream for the contacts, which run beside IBB, with its fork/join events
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_contacts = nullptr;
     void *f[2] = {nullptr, nullptr}, *g[2] = {nullptr, nullptr};
     int cur = 0;
     int phase = PHASE_HOME;
