@@ -47,9 +47,10 @@ NCU_DRAM_BYTES = {"f64": 7.30e9 + 7.16e9, "f32": 3.68e9 + 3.69e9, "f16s": 1.90e9
 
 def bytes_per_node(storage: int) -> int:
     """Algorithmic HBM bytes per lattice-node update: read+write 27 f and 27 g populations plus
-    read+write of the FP64 buoyancy auxiliary F_x."""
+    read+write of the buoyancy auxiliary F_x (FP64 with FP64 storage; FP32 with the float storage
+    modes, which compute F_x in FP32): 880, 440 and 224 bytes."""
     s = {0: 8, 1: 4, 2: 2}[storage]
-    return 2 * 54 * s + 2 * 8
+    return 2 * 54 * s + 2 * (8 if storage == 0 else 4)
 
 
 def hbm_peak():

@@ -85,6 +85,28 @@ int read_status(rbtp_handle *h)
     return RBTP_OK;
 }
 
+// The F_x auxiliary to and from host FP64 (it is FP32 on the device in the float storage modes,
+// where the step computes F_x in FP32, so both directions are exact).  Synchronous.
+cudaError_t aux_to_host(const rbtp_handle *h, double *dst)
+{
+    const size_t L = (size_t)h->geo.L;
+    if (h->mode == RBTP_STORE_F64) return cudaMemcpy(dst, h->faux, L * sizeof(double), cudaMemcpyDeviceToHost);
+    std::vector<float> tmp(L);
+    const cudaError_t e = cudaMemcpy(tmp.data(), h->faux, L * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    for (size_t k = 0; k < L; ++k) dst[k] = (double)tmp[k];
+    return cudaSuccess;
+}
+
+cudaError_t aux_from_host(rbtp_handle *h, const double *src)
+{
+    const size_t L = (size_t)h->geo.L;
+    if (h->mode == RBTP_STORE_F64) return cudaMemcpy(h->faux, src, L * sizeof(double), cudaMemcpyHostToDevice);
+    std::vector<float> tmp(L);
+    for (size_t k = 0; k < L; ++k) tmp[k] = (float)src[k];
+    return cudaMemcpy(h->faux, tmp.data(), L * sizeof(float), cudaMemcpyHostToDevice);
+}
+
 // Build the current solid flags and the IBB link slabs from the current particle positions
 // (build_links, links.cu:572-685).
 int build_links(rbtp_handle *h, int *owner)
@@ -512,7 +534,7 @@ int rbtp_load_state(rbtp_handle *h, const double *f, const double *g, const doub
         CK(cudaMemsetAsync(h->ted, 0, L * sizeof(double), h->stream));
         CK(cudaMemsetAsync(h->ked, 0, L * sizeof(double), h->stream));
     }
-    CK(launch_forcing(h->geo, h->ph, h->phi, h->faux, h->stream));
+    CK(launch_forcing(h->mode, h->geo, h->ph, h->phi, h->faux, h->stream));
     h->istep = h->cfg.continuous_steps > 0 ? h->cfg.continuous_steps : 0;
     h->initialised = true;
     h->macros_valid = true;
@@ -576,7 +598,7 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
         h->plane_valid = false;
         h->macros_valid = macro;
         if (flow) {
-            CK(launch_dissipation(h->geo, h->ph, h->fcol, h->gcol, h->rho, h->ux, h->uy, h->uz, h->phi,
+            CK(launch_dissipation(h->mode, h->geo, h->ph, h->fcol, h->gcol, h->rho, h->ux, h->uy, h->uz, h->phi,
                                   h->faux, parts ? h->owner[h->ocur] : nullptr, h->ted, h->ked, h->stream));
             h->dissip_valid = true;
         } else {
@@ -620,8 +642,8 @@ int rbtp_get_macros(rbtp_handle *h, double *rho, double *ux, double *uy, double 
     if (uy) CK(cudaMemcpyAsync(uy, h->uy, n, cudaMemcpyDeviceToHost, h->stream));
     if (uz) CK(cudaMemcpyAsync(uz, h->uz, n, cudaMemcpyDeviceToHost, h->stream));
     if (phi) CK(cudaMemcpyAsync(phi, h->phi, n, cudaMemcpyDeviceToHost, h->stream));
-    if (force_x) CK(cudaMemcpyAsync(force_x, h->faux, n, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    if (force_x) CK(aux_to_host(h, force_x));
     return RBTP_OK;
 }
 
@@ -1141,7 +1163,7 @@ int rbtp_checkpoint_write(rbtp_handle *h, const char *path)
         }
         ok = std::fwrite(pop.data(), 1, P, fp) == P;
     }
-    if (cudaMemcpy(aux.data(), h->faux, L * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+    if (aux_to_host(h, aux.data()) != cudaSuccess ||
         cudaMemcpy(wall.data(), h->rho_wall, W * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
         std::fclose(fp);
         return fail(h, RBTP_ERR_CUDA, "checkpoint read-back failed");
@@ -1203,7 +1225,8 @@ int rbtp_checkpoint_read(rbtp_handle *h, const char *path)
         CK(cudaMemcpyAsync(h->f[0], f.data(), P, cudaMemcpyHostToDevice, h->stream));
         CK(cudaMemcpyAsync(h->g[0], g.data(), P, cudaMemcpyHostToDevice, h->stream));
     }
-    CK(cudaMemcpyAsync(h->faux, aux.data(), L * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(aux_from_host(h, aux.data()));
     CK(cudaMemcpyAsync(h->rho_wall, wall.data(), W * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     if (hd.macros_valid) {
         double *dst[5] = {h->rho, h->ux, h->uy, h->uz, h->phi};

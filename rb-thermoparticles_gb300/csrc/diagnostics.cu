@@ -130,13 +130,14 @@ __global__ void k_batch_sample_final(const CavDesc *desc)
 // the step's post-collision populations; solid nodes are then zeroed as output_flow does.
 __global__ void k_dissipation(const Geo geo, const Phys ph, const double *fcol, const double *gcol,
                               const double *rho, const double *ux, const double *uy,
-                              const double *uz, const double *phi, const double *faux,
+                              const double *uz, const double *phi, const void *faux, bool aux32,
                               const int *owner, double *ted, double *ked)
 {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= geo.L) return;
     const long long L = geo.L;
-    const double fx = faux[idx], fy = 0.0, fz = 0.0;
+    const double fx = aux32 ? (double)static_cast<const float *>(faux)[idx] : static_cast<const double *>(faux)[idx];
+    const double fy = 0.0, fz = 0.0;
     const double r = rho[idx], ph_ = phi[idx];
     const double u = ux[idx], v = uy[idx], w = uz[idx];
     const double RT = 1.0 / 3.0;
@@ -202,13 +203,14 @@ cudaError_t launch_plane_sums(const Geo &geo, const Phys &ph, const double *ux, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_dissipation(const Geo &geo, const Phys &ph, const double *fcol,
+cudaError_t launch_dissipation(int mode, const Geo &geo, const Phys &ph, const double *fcol,
                                const double *gcol, const double *rho, const double *ux,
                                const double *uy, const double *uz, const double *phi,
-                               const double *faux, const int *owner, double *ted, double *ked,
+                               const void *faux, const int *owner, double *ted, double *ked,
                                cudaStream_t st)
 {
-    k_dissipation<<<(unsigned)((geo.L + 127) / 128), 128, 0, st>>>(geo, ph, fcol, gcol, rho, ux, uy, uz, phi, faux, owner, ted, ked);
+    k_dissipation<<<(unsigned)((geo.L + 127) / 128), 128, 0, st>>>(geo, ph, fcol, gcol, rho, ux, uy, uz, phi, faux,
+                                                                   mode != RBTP_STORE_F64, owner, ted, ked);
     return cudaGetLastError();
 }
 

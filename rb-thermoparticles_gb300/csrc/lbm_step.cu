@@ -128,7 +128,7 @@ __global__ void k_home_import(const Geo geo, const Phys ph, const double *fin, c
 // init_f / init_g (initial.cu:335-397): deviation-form rest f = 0; g from the equilibrium at
 // T = T_REF with the rho field that init_f set to RHO0.
 template <int MODE>
-__global__ void k_fresh_init(const Geo geo, const Phys ph, void *f_, void *g_, double *faux,
+__global__ void k_fresh_init(const Geo geo, const Phys ph, void *f_, void *g_, void *faux_,
                              double *rho, double *ux, double *uy, double *uz, double *phi)
 {
     using ST = Store<MODE>;
@@ -144,7 +144,7 @@ __global__ void k_fresh_init(const Geo geo, const Phys ph, void *f_, void *g_, d
     rho[n] = ph.rho0;
     ux[n] = 0.0; uy[n] = 0.0; uz[n] = 0.0;
     phi[n] = tT;
-    faux[n] = ph.grav0 * ph.beta * (tT - ph.t0);
+    static_cast<typename ST::A *>(faux_)[n] = (typename ST::A)(ph.grav0 * ph.beta * (tT - ph.t0));
     unroll<27>([&](auto I) {
         constexpr int i = decltype(I)::value;
         constexpr double w = dweight(i);
@@ -176,11 +176,13 @@ __global__ void k_macros_from_home(const Geo geo, const double *f, const double 
     rho[n] = r; ux[n] = jx; uy[n] = jy; uz[n] = jz; phi[n] = p;
 }
 
-__global__ void k_forcing(const Geo geo, const Phys ph, const double *phi, double *faux)
+template <int MODE>
+__global__ void k_forcing(const Geo geo, const Phys ph, const double *phi, void *faux)
 {
     const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= geo.L) return;
-    faux[n] = ph.grav0 * ph.beta * (phi[n] - ph.t0);
+    using A = typename Store<MODE>::A;
+    static_cast<A *>(faux)[n] = (A)(ph.grav0 * ph.beta * (phi[n] - ph.t0));
 }
 
 inline dim3 node_grid(const Geo &g, dim3 blk)
@@ -258,7 +260,7 @@ cudaError_t launch_home_import(int mode, const Geo &geo, const Phys &ph, const d
 }
 
 cudaError_t launch_fresh_init(int mode, const Geo &geo, const Phys &ph, void *f, void *g,
-                              double *faux, double *rho, double *ux, double *uy, double *uz,
+                              void *faux, double *rho, double *ux, double *uy, double *uz,
                               double *phi, cudaStream_t st)
 {
     RBTP_MODE_DISPATCH(mode, (k_fresh_init<M><<<lin_blocks(geo.L, 256), 256, 0, st>>>(geo, ph, f, g, faux, rho, ux, uy, uz, phi)));
@@ -273,10 +275,10 @@ cudaError_t launch_macros_from_home(const Geo &geo, const double *f, const doubl
     return cudaGetLastError();
 }
 
-cudaError_t launch_forcing(const Geo &geo, const Phys &ph, const double *phi, double *faux,
+cudaError_t launch_forcing(int mode, const Geo &geo, const Phys &ph, const double *phi, void *faux,
                            cudaStream_t st)
 {
-    k_forcing<<<lin_blocks(geo.L, 256), 256, 0, st>>>(geo, ph, phi, faux);
+    RBTP_MODE_DISPATCH(mode, (k_forcing<M><<<lin_blocks(geo.L, 256), 256, 0, st>>>(geo, ph, phi, faux)));
     return cudaGetLastError();
 }
 

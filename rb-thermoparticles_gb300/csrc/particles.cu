@@ -1243,7 +1243,7 @@ __global__ void k_refill_compute(const Geo geo, const Phys ph, const PartBuffers
 // Scatter the refill values into the slots the next pull reads at each new-fluid node.
 template <int MODE>
 __device__ __forceinline__ void refill_scatter_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                                                    void *f_, void *g_, double *faux,
+                                                    void *f_, void *g_, void *faux,
                                                     const double *rho_wall, bool macros, double *rho,
                                                     double *ux, double *uy, double *uz, double *phi,
                                                     const DevStatus *status, long long t0, long long stride)
@@ -1286,7 +1286,7 @@ __device__ __forceinline__ void refill_scatter_body(const Geo &geo, const Phys &
             ST::st_g(gB + (long long)o * L + idx, (R)gs, w, gshift(ph, ix));
         }
         if (ip == 0) {
-            faux[idx] = 0.0;
+            static_cast<typename Store<MODE>::A *>(faux)[idx] = 0;
             if (macros) {
                 const double *m = pb.nf_mac + (long long)n * 5;
                 rho[idx] = m[0]; ux[idx] = m[1]; uy[idx] = m[2]; uz[idx] = m[3]; phi[idx] = m[4];
@@ -1297,7 +1297,7 @@ __device__ __forceinline__ void refill_scatter_body(const Geo &geo, const Phys &
 
 template <int MODE>
 __global__ void k_refill_scatter(const Geo geo, const Phys ph, const PartBuffers pb, void *f_,
-                                 void *g_, double *faux, const double *rho_wall, bool macros,
+                                 void *g_, void *faux, const double *rho_wall, bool macros,
                                  double *rho, double *ux, double *uy, double *uz, double *phi,
                                  const DevStatus *status)
 {
@@ -1383,7 +1383,7 @@ cudaError_t launch_link_fill(int mode, const Geo &geo, const Phys &ph, const Par
 
 cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
                           const int *owner_prev, const int *owner_cur, void *f, void *g,
-                          double *faux, const double *rho_wall, bool macros, double *rho,
+                          void *faux, const double *rho_wall, bool macros, double *rho,
                           double *ux, double *uy, double *uz, double *phi, DevStatus *status,
                           cudaStream_t st)
 {

@@ -133,9 +133,12 @@ __host__ __device__ __forceinline__ void unroll(F &&f)
 // of both populations of a direction is one 8- or 4-byte access; the f and g buffer pointers of
 // such a handle are the same allocation, and ld_f/ld_g/st_f/st_g address the halves of a slot.
 template <int MODE> struct Store;
+// A: type of the per-node F_x auxiliary (the step stores the F_x it computed in its working
+// precision R, so the stored value is exact in every mode).
 template <> struct Store<RBTP_STORE_F64> {
     using S = double;
     using R = double;
+    using A = double;
     static constexpr bool PAIRED = false;
     static __device__ __forceinline__ R ld_f(const S *p, double, double) { return *p; }
     static __device__ __forceinline__ R ld_g(const S *p, double, double) { return *p; }
@@ -145,6 +148,7 @@ template <> struct Store<RBTP_STORE_F64> {
 template <> struct Store<RBTP_STORE_F32> {
     using S = float2;   // (f_i, g_i)
     using R = float;
+    using A = float;
     static constexpr bool PAIRED = true;
     static __device__ __forceinline__ R ld_f(const S *p, double, double) { return p->x; }
     static __device__ __forceinline__ R ld_g(const S *p, double, double) { return p->y; }
@@ -157,6 +161,7 @@ template <> struct Store<RBTP_STORE_F32> {
 template <> struct Store<RBTP_STORE_F16S> {
     using S = __half2;  // (f_i / w_i, g_i / w_i - T_c(x))
     using R = float;
+    using A = float;
     static constexpr bool PAIRED = true;
     // w: lattice weight of the slot's direction
     static __device__ __forceinline__ R ld_f(const S *p, double w, double) { return __low2float(*p) * (float)w; }
@@ -274,7 +279,7 @@ enum StepOut { OUT_NONE = 0, OUT_RHO = 1, OUT_MACROS = 2, OUT_MACROS_COL = 3, OU
 struct StepBuffers {
     const void *fin, *gin;
     void *fout, *gout;
-    double *faux;       // F_x of the previous step in, F_x of this step out (L)
+    void *faux;         // F_x of the previous step in, F_x of this step out (L of Store<MODE>::A)
     double *rho_wall;   // density deviation at the x = 0 and x = LX-1 planes (2*LY*LZ)
     double *rho, *ux, *uy, *uz, *phi;   // macro outputs (L each), may be null
     double *fcol, *gcol;                // FP64 copy of the post-collision populations, may be null
@@ -291,12 +296,12 @@ cudaError_t launch_home_export(int mode, const Geo &geo, const Phys &ph, const v
 cudaError_t launch_home_import(int mode, const Geo &geo, const Phys &ph, const double *fin,
                                const double *gin, void *fout, void *gout, cudaStream_t st);
 cudaError_t launch_fresh_init(int mode, const Geo &geo, const Phys &ph, void *f, void *g,
-                              double *faux, double *rho, double *ux, double *uy, double *uz,
+                              void *faux, double *rho, double *ux, double *uy, double *uz,
                               double *phi, cudaStream_t st);
 cudaError_t launch_macros_from_home(const Geo &geo, const double *f, const double *g, double *rho,
                                     double *ux, double *uy, double *uz, double *phi,
                                     cudaStream_t st);
-cudaError_t launch_forcing(const Geo &geo, const Phys &ph, const double *phi, double *faux,
+cudaError_t launch_forcing(int mode, const Geo &geo, const Phys &ph, const double *phi, void *faux,
                            cudaStream_t st);
 
 // Particle pipeline ------------------------------------------------------------------------------
@@ -364,7 +369,7 @@ cudaError_t launch_link_fill(int mode, const Geo &geo, const Phys &ph, const Par
                              const int *owner, DevStatus *status, cudaStream_t st);
 cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
                           const int *owner_prev, const int *owner_cur, void *f, void *g,
-                          double *faux, const double *rho_wall, bool macros, double *rho,
+                          void *faux, const double *rho_wall, bool macros, double *rho,
                           double *ux, double *uy, double *uz, double *phi, DevStatus *status,
                           cudaStream_t st);
 cudaError_t launch_initial_owner(const Geo &geo, const Phys &ph, const PartBuffers &pb,
@@ -379,7 +384,8 @@ struct CavDesc {
     Geo geo;
     Phys ph;
     void *f[2], *g[2];
-    double *faux, *rho_wall, *rho, *ux, *uy, *uz, *phi;
+    void *faux;                         // F_x auxiliary (Store<MODE>::A)
+    double *rho_wall, *rho, *ux, *uy, *uz, *phi;
     DevStatus *status;
     PartBuffers pb;
     int *owner[2];
@@ -415,10 +421,10 @@ cudaError_t launch_plane_sums(const Geo &geo, const Phys &ph, const double *ux, 
                               double *plane, cudaStream_t st);
 // Batched sampling: plane sums of every cavity whose samp_now is set, into its sample ring.
 cudaError_t launch_batch_sample(const CavDesc *desc, int n, cudaStream_t st);
-cudaError_t launch_dissipation(const Geo &geo, const Phys &ph, const double *fcol,
+cudaError_t launch_dissipation(int mode, const Geo &geo, const Phys &ph, const double *fcol,
                                const double *gcol, const double *rho, const double *ux,
                                const double *uy, const double *uz, const double *phi,
-                               const double *faux, const int *owner, double *ted, double *ked,
+                               const void *faux, const int *owner, double *ted, double *ked,
                                cudaStream_t st);
 
 }  // namespace rbtp

@@ -64,6 +64,9 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
             gv = v.y;
         }
     };
+    // F_x of the previous step, read ahead of the population gather
+    using A = typename ST::A;
+    const A fold_in = __ldg(static_cast<const A *>(b.faux) + node);
     R f[27], g[27];
     // INTERIOR: no neighbour of this warp's nodes leaves the box, so every pull is the plain
     // f*_i(x - c_i) (the face tests and the bounce-back selects drop out)
@@ -208,11 +211,11 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     }
     if (!(fabs(rho) < (R)1e30) || !(fabs(phi) < (R)1e30)) atomicOr(&b.status->nonfinite, 1);
 
-    const R fold = (R)b.faux[node];
+    const R fold = (R)fold_in;
     const R ux = jx + (R)0.5 * fold, uy = jy, uz = jz;
     // forcing (macrovar.cu:45): F_x = g0 beta (phi - T0); F_y = F_z = 0 always
     const R Fx = K.g0b * (phi - K.t0);
-    b.faux[node] = (double)Fx;
+    static_cast<A *>(b.faux)[node] = (A)Fx;
 
     if constexpr (OUT >= OUT_MACROS) {
         b.rho[node] = (double)rho;
