@@ -195,7 +195,10 @@ template <int MODE>
 cudaError_t launch_step_mode(bool pull, int out, const Geo &geo, const Phys &ph,
                              const StepBuffers &b, cudaStream_t st)
 {
-    const dim3 blk(32, 4, 1);
+    // warps of 32 x-nodes in one row (FP64, FP32); 16 x 2 for shifted FP16, which is issue-bound:
+    // half as many warps hold an x-face node and take the bounce-back gather (-1.4 % time at
+    // 320x320x160; FP32, HBM-bound, is 1.7 % slower with it)
+    const dim3 blk = MODE == RBTP_STORE_F16S ? dim3(16, 8, 1) : dim3(32, 4, 1);
     const dim3 grd = node_grid(geo, blk);
 #define RBTP_STEP_CASE(P, O)                                                       \
     if (pull == P && out == O) {                                                   \

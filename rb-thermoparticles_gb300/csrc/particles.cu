@@ -460,8 +460,9 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
         auto add = [&](int k, float v) { sum[k] = df_add(sum[k], df{v, 0.0f}); };
         // (f_i, g_i) slots of the paired layout: both populations of a slot in one access;
         // shifted-FP16 g holds g / w - T_c(x_home), the slot's home node x-index gives the shift
+        // (read-only path: a link reads only slots of fluid nodes, which no link writes)
         auto ld2 = [&](const S *ptr, int ixh, float wr, float &fv, float &gv) {
-            const S v = *ptr;
+            const S v = __ldg(ptr);
             if constexpr (MODE == RBTP_STORE_F16S) {
                 fv = __low2float(v) * wr;
                 gv = (__high2float(v) + (tla + tlb * (float)ixh)) * wr;
@@ -481,10 +482,10 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             bool fluid1;
         };
         auto gather = [&](int t, LinkIn &a) {
-            a.x = pb.link_node[base + t];
-            const int dw = pb.link_dir[base + t];
+            a.x = __ldg(pb.link_node + base + t);
+            const int dw = __ldg(pb.link_dir + base + t);
             a.ip = dw & LINK_DIR_MASK;
-            a.q = (float)pb.link_q[base + t];
+            a.q = (float)__ldg(pb.link_q + base + t);
             a.fluid1 = (dw >> LINK_UP) & 1;   // upstream node x - c_ip is in-domain fluid
             const int ip = a.ip, x = a.x;
             const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
@@ -509,7 +510,7 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
                     if (a.q > 0.5f) a.g_2 = go;
                 }
             }
-            a.rho = (float)rho[x];
+            a.rho = (float)__ldg(rho + x);
         };
         auto finish = [&](const LinkIn &a) {
             const int x = a.x, ip = a.ip;
