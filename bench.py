@@ -42,7 +42,7 @@ FALLBACK_HBM_GBS = 6800.0
 # `python bench.py --only production:<storage> --steps 3 --warmup 3`
 # (profiles/k_step_dram_320x320x160.md).  Algorithmic bytes per launch: 16,384,000 nodes x
 # bytes_per_node.
-NCU_DRAM_BYTES = {"f64": 7.30e9 + 7.16e9, "f32": 3.68e9 + 3.69e9, "f16s": 1.90e9 + 1.86e9}
+NCU_DRAM_BYTES = {"f64": 7.30e9 + 7.16e9, "f32": 3.62e9 + 3.63e9, "f16s": 1.84e9 + 1.80e9}
 
 
 def bytes_per_node(storage: int) -> int:
