@@ -715,6 +715,7 @@ int rbtp_get_links(rbtp_handle *h, int *n, int *node, int *dir, int *pid, double
         if (pid) pid[k] = all[k].pid;
         if (q) q[k] = all[k].q;
     }
+    *n = (int)all.size();
     return RBTP_OK;
 }
 

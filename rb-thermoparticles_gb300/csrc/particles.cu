@@ -919,8 +919,10 @@ __global__ void __launch_bounds__(NT) k_mark(const Geo geo, const Phys ph, const
 // mask per node); an exclusive scan of the mask popcounts numbers the candidates (node, direction)
 // in node-then-direction order.  Phase 2: candidate k is located by a binary search over the scan
 // and a bit select in its node's mask, the ray-sphere q of links.cu:7-23 runs with all lanes busy,
-// and accepted links are appended to the particle's slab in the same order (the reference's
-// (idx, ip) order, links.cu:221-250).  Only the spherical shell that can hold link nodes is
+// and candidate k goes to slab entry base + k, so the slab holds the links in the reference's
+// (idx, ip) order (links.cu:221-250).  A candidate whose ray-sphere test fails (a grazing ray
+// rounded off the sphere) is rare; a block vote finds the groups that hold one, and only those
+// are compacted by a block scan.  Only the spherical shell that can hold link nodes is
 // enumerated: per (y, z) row of the box, the x-intervals between an inner radius (nodes inside it
 // are certainly solid) and the outer reach r + 2, with float margins so that every possible link
 // node is kept; rows are numbered by a block scan and flat indices are mapped back by a binary
@@ -1052,8 +1054,13 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
                                 PCOL(st, pb.np, 2, p), dmul(ph.radius, ph.radius), q) ? 1 : 0;
                 }
             }
-            int ltotal;
-            const int lpos = base + block_exclusive_scan<NT>(ok, sm.rows.wsum, ltotal);
+            int lpos, ltotal;
+            if (__syncthreads_or(k < ccount && !ok)) {
+                lpos = base + block_exclusive_scan<NT>(ok, sm.rows.wsum, ltotal);
+            } else {
+                lpos = base + threadIdx.x;   // every candidate of the group is a link
+                ltotal = min(NT, ccount - k0);
+            }
             if (ok) {
                 if (lpos < pb.link_cap) {
                     pb.link_node[slab + lpos] = node;

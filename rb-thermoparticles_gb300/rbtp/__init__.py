@@ -337,7 +337,8 @@ class Solver:
         node, d, pid = (np.empty(k, dtype=np.int32) for _ in range(3))
         q = np.empty(k)
         _check(self.lib.rbtp_get_links(self._h, C.byref(n), _ip(node), _ip(d), _ip(pid), _dp(q), k), self._h)
-        return node, d, pid, q
+        k = n.value
+        return node[:k], d[:k], pid[:k], q[:k]
 
     def new_fluid(self):
         n = C.c_int()
