@@ -301,7 +301,7 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
     {
         CKC(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
         CKC(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
-        CKC(cudaEventCreateWithFlags(&h->ev_contacts, cudaEventDisableTiming));
+        CKC(cudaEventCreateWithFlags(&h->ev_side, cudaEventDisableTiming));
     }
     const size_t sb = store_bytes(h->mode);
     const size_t P = (size_t)27 * (size_t)L;
@@ -403,7 +403,7 @@ int rbtp_destroy(rbtp_handle *h)
     cudaFree(pb.cell_count); cudaFree(pb.cell_start); cudaFree(pb.cell_fill); cudaFree(pb.cell_items);
     cudaFree(pb.pair_p); cudaFree(pb.pair_q);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
-    if (h->ev_contacts) cudaEventDestroy(h->ev_contacts);
+    if (h->ev_side) cudaEventDestroy(h->ev_side);
     if (h->side) cudaStreamDestroy(h->side);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -581,9 +581,9 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
             CK(cudaEventRecord(h->ev_fork, h->stream));
             CK(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
             CK(launch_contacts(h->geo, h->ph, h->pb, h->status, h->side));
-            CK(cudaEventRecord(h->ev_contacts, h->side));
+            CK(cudaEventRecord(h->ev_side, h->side));
             CK(launch_links_ibb(h->mode, h->geo, h->ph, h->pb, h->f[dst], h->g[dst], h->rho, h->stream));
-            CK(cudaStreamWaitEvent(h->stream, h->ev_contacts, 0));
+            CK(cudaStreamWaitEvent(h->stream, h->ev_side, 0));
             CK(launch_update(h->ph, h->pb, h->stream));
             s = build_links(h, on);
             if (s) return s;

@@ -31,7 +31,7 @@ struct rbtp_handle {
     cudaStream_t stream = nullptr;
     // particle steps: side stream for the contacts, which run beside IBB, with its fork/join events
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_contacts = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_side = nullptr;
     void *f[2] = {nullptr, nullptr}, *g[2] = {nullptr, nullptr};
     int cur = 0;
     int phase = PHASE_HOME;
