@@ -28,6 +28,9 @@ struct rbtp_batch {
     int sms = 1;
     cudaStream_t stream = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
+    // side branch of each step (the contact kernels beside IBB) and its fork/join events
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<rbtp_handle *> members;
     CavDesc *d_desc = nullptr, *h_desc = nullptr;
     int desc_cap = 0;
@@ -198,7 +201,7 @@ cudaError_t enqueue_step(rbtp_batch *b, int shape, int grid)
     if ((e = launch_step_batched(b->mode, shape, b->d_desc, b->d_tiles[shape], b->ntiles[shape], grid, b->stream)))
         return e;
     if ((e = launch_particles_batched(b->mode, b->d_desc, b->d_pmap, b->total_np, b->d_cmap, b->ncmap, b->d_pmem,
-                                        b->npmem, b->stream)))
+                                        b->npmem, b->stream, b->side, b->ev_fork, b->ev_join)))
         return e;
     if ((e = launch_batch_advance(b->d_desc, n, b->stream))) return e;
     return launch_batch_sample(b->d_desc, n, b->stream);
@@ -276,7 +279,10 @@ int rbtp_batch_create(int storage, rbtp_batch **out)
     cudaGetDevice(&b->device);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
     if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess) {
+        cudaEventCreate(&b->e0) != cudaSuccess || cudaEventCreate(&b->e1) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess) {
         rbtp_batch_destroy(b);
         return RBTP_ERR_CUDA;
     }
@@ -299,6 +305,9 @@ int rbtp_batch_destroy(rbtp_batch *b)
     if (b->h_desc) cudaFreeHost(b->h_desc);
     if (b->e0) cudaEventDestroy(b->e0);
     if (b->e1) cudaEventDestroy(b->e1);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
+    if (b->side) cudaStreamDestroy(b->side);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return RBTP_OK;

@@ -1591,7 +1591,8 @@ __global__ void k_refill_scatter_b(const CavDesc *desc, const int *pmem)
 
 template <int MODE>
 cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int total, const int2 *cmap,
-                                   int ncmap, const int *pmem, int npmem, cudaStream_t st)
+                                   int ncmap, const int *pmem, int npmem, cudaStream_t st, cudaStream_t side,
+                                   cudaEvent_t ev_fork, cudaEvent_t ev_join)
 {
     const int t = 128, bl = (total + t - 1) / t;
     cudaError_t e;
@@ -1599,13 +1600,18 @@ cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int to
     do {                                                                    \
         if ((e = pdl_launch(__VA_ARGS__)) != cudaSuccess) return e;         \
     } while (0)
-    RBTP_PDL(k_links_ibb_b<MODE>, dim3(ncmap), dim3(IBB_THREADS), st, desc, pmap, cmap);
-    RBTP_PDL(k_cells_zero_b, dim3(4, npmem), dim3(256), st, desc, pmem);
-    RBTP_PDL(k_cell_count_b, dim3(bl), dim3(t), st, desc, pmap, total);
-    RBTP_PDL(k_cell_scan_b, dim3(npmem), dim3(1024), st, desc, pmem);
-    RBTP_PDL(k_cell_fill_b, dim3(bl), dim3(t), st, desc, pmap, total);
-    RBTP_PDL(k_contact_force_b, dim3((total + CONTACT_WARPS - 1) / CONTACT_WARPS), dim3(32 * CONTACT_WARPS), st,
+    // contacts (cell list and pair forces of the current positions) beside IBB
+    if ((e = cudaEventRecord(ev_fork, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(side, ev_fork, 0)) != cudaSuccess) return e;
+    RBTP_PDL(k_cells_zero_b, dim3(4, npmem), dim3(256), side, desc, pmem);
+    RBTP_PDL(k_cell_count_b, dim3(bl), dim3(t), side, desc, pmap, total);
+    RBTP_PDL(k_cell_scan_b, dim3(npmem), dim3(1024), side, desc, pmem);
+    RBTP_PDL(k_cell_fill_b, dim3(bl), dim3(t), side, desc, pmap, total);
+    RBTP_PDL(k_contact_force_b, dim3((total + CONTACT_WARPS - 1) / CONTACT_WARPS), dim3(32 * CONTACT_WARPS), side,
              desc, pmap, total);
+    if ((e = cudaEventRecord(ev_join, side)) != cudaSuccess) return e;
+    RBTP_PDL(k_links_ibb_b<MODE>, dim3(ncmap), dim3(IBB_THREADS), st, desc, pmap, cmap);
+    if ((e = cudaStreamWaitEvent(st, ev_join, 0)) != cudaSuccess) return e;
     RBTP_PDL(k_update_b, dim3(bl), dim3(t), st, desc, pmap, total);
     RBTP_PDL(k_owner_fill_b, dim3(64, npmem), dim3(256), st, desc, pmem);
     RBTP_PDL(k_pgeo_b, dim3(bl), dim3(t), st, desc, pmap, total);
@@ -1627,13 +1633,17 @@ cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int to
 }  // namespace
 
 cudaError_t launch_particles_batched(int mode, const CavDesc *desc, const int2 *pmap, int total_np,
-                                     const int2 *cmap, int ncmap, const int *pmem, int npmem, cudaStream_t st)
+                                     const int2 *cmap, int ncmap, const int *pmem, int npmem, cudaStream_t st,
+                                     cudaStream_t side, cudaEvent_t ev_fork, cudaEvent_t ev_join)
 {
     if (total_np <= 0 || npmem <= 0) return cudaSuccess;
     switch (mode) {
-    case RBTP_STORE_F64: return particles_batched_mode<RBTP_STORE_F64>(desc, pmap, total_np, cmap, ncmap, pmem, npmem, st);
-    case RBTP_STORE_F32: return particles_batched_mode<RBTP_STORE_F32>(desc, pmap, total_np, cmap, ncmap, pmem, npmem, st);
-    case RBTP_STORE_F16S: return particles_batched_mode<RBTP_STORE_F16S>(desc, pmap, total_np, cmap, ncmap, pmem, npmem, st);
+    case RBTP_STORE_F64:
+        return particles_batched_mode<RBTP_STORE_F64>(desc, pmap, total_np, cmap, ncmap, pmem, npmem, st, side, ev_fork, ev_join);
+    case RBTP_STORE_F32:
+        return particles_batched_mode<RBTP_STORE_F32>(desc, pmap, total_np, cmap, ncmap, pmem, npmem, st, side, ev_fork, ev_join);
+    case RBTP_STORE_F16S:
+        return particles_batched_mode<RBTP_STORE_F16S>(desc, pmap, total_np, cmap, ncmap, pmem, npmem, st, side, ev_fork, ev_join);
     }
     return cudaErrorInvalidValue;
 }

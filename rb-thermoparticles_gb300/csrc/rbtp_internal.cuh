@@ -409,8 +409,11 @@ cudaError_t launch_batch_plan(CavDesc *desc, int n, cudaStream_t st);
 cudaError_t launch_batch_advance(CavDesc *desc, int n, cudaStream_t st);
 cudaError_t launch_step_batched(int mode, int shape, const CavDesc *desc, const int4 *tiles,
                                 int ntiles, int grid, cudaStream_t st);
+// The contact kernels (positions only) run on `side` beside IBB: forked after `ev_fork` is recorded
+// on st, joined through `ev_join` before the integrator.
 cudaError_t launch_particles_batched(int mode, const CavDesc *desc, const int2 *pmap, int total_np,
-                                     const int2 *cmap, int ncmap, const int *pmem, int npmem, cudaStream_t st);
+                                     const int2 *cmap, int ncmap, const int *pmem, int npmem, cudaStream_t st,
+                                     cudaStream_t side, cudaEvent_t ev_fork, cudaEvent_t ev_join);
 
 // Diagnostics ------------------------------------------------------------------------------------
 // Per-x-plane sums: 10 quantities x lx, see diagnostics.cu.
