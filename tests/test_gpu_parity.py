@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from conftest import rel_l2
-from rbtp import Solver, RbtpError, STORE_F32, STORE_F16S, workloads as W
+from rbtp import Solver, RbtpError, STORE_F32, STORE_F16S, derive, workloads as W
 
 pytestmark = pytest.mark.gpu
 
@@ -188,6 +188,88 @@ def test_many_particles_take_the_narrow_launch_path(env):
     o.step(10)
     _compare_fields(s, o)
     assert np.array_equal(s.flags(), o.flags())
+
+
+def _rejected_candidates(env, X, r):
+    """Candidates (fluid node, direction whose neighbour lies in the sphere) of one isolated sphere
+    that fail the reference's ray-sphere test (links.cu:7-23) on rounding."""
+    rsq = r * r
+    lo, hi = np.floor(X - r - 2).astype(int), np.ceil(X + r + 2).astype(int)
+    out = []
+    for ix in range(lo[0], hi[0] + 1):
+        for iy in range(lo[1], hi[1] + 1):
+            for iz in range(lo[2], hi[2] + 1):
+                x0, y0, z0 = ix + 0.5, iy + 0.5, iz + 0.5
+                dx, dy, dz = x0 - X[0], y0 - X[1], z0 - X[2]
+                if dx * dx + dy * dy + dz * dz <= rsq:
+                    continue
+                for ip in range(1, 27):
+                    ex, ey, ez = x0 + W.CX[ip] - X[0], y0 + W.CY[ip] - X[1], z0 + W.CZ[ip] - X[2]
+                    if ex * ex + ey * ey + ez * ez > rsq:
+                        continue
+                    if not env.link_q(ip, x0, y0, z0, X[0], X[1], X[2], rsq)[0]:
+                        out.append((ix, iy, iz, ip))
+    return out
+
+
+def _rejecting_spheres(env, r, nodes, rng):
+    """Centres X = n + 1/2 - r u (u a random unit vector) put the node centre n on the sphere up to
+    rounding; kept when some candidate ray then rounds to q just above 1 and is rejected."""
+    out = []
+    for n in nodes:
+        for _ in range(400):
+            u = rng.standard_normal(3)
+            X = np.asarray(n, dtype=float) + 0.5 - r * u / np.linalg.norm(u)
+            if _rejected_candidates(env, X, r):
+                out.append(X)
+                break
+    return out
+
+
+@pytest.mark.parametrize("storage", [0, STORE_F32])
+@pytest.mark.parametrize("narrow", [False, True])
+def test_links_with_rejected_candidates(env, narrow, storage):
+    """Spheres placed so that candidate rays round off the surface: the link build's compaction
+    path (taken only by candidate groups that hold a rejected ray) gives the oracle's link set on
+    both launch widths (512-thread CTAs below 608 spheres, 128 above) and in FP64 and FP32
+    storage."""
+    if narrow:
+        v = 4.0 * math.pi * 2.0 ** 3 / 3.0
+        cfg = _particle_cfg(lx=96, ly=96, lz=48, particle_diam_frac=4.0 / 96.0,
+                            particle_fraction=700.5 * v / (96 * 96 * 48), storage=storage)
+        nodes = [(8 + 9 * a, 8 + 9 * b, 24) for a in range(2) for b in range(8)]
+        free_x = (30.0, 92.0)
+    else:
+        cfg = _particle_cfg(particle_fraction=0.01, storage=storage)
+        nodes = [(10, 12 + 14 * b, 16) for b in range(3)] + [(24, 12 + 14 * b, 16) for b in range(3)]
+        free_x = (38.0, 58.0)
+    s, o = _pair(env, cfg)
+    n = s.npart
+    r = float(derive(cfg).particle_radius)
+    rng = np.random.default_rng(11)
+    placed = _rejecting_spheres(env, r, nodes[:n], rng)
+    assert len(placed) >= min(3, n)
+    p = np.zeros((n, 33))
+    p[:, 30] = 0.5
+    p[:len(placed), :3] = placed
+    rest = n - len(placed)
+    p[len(placed):, 0] = rng.uniform(*free_x, rest)
+    p[len(placed):, 1] = rng.uniform(r + 1, cfg.ly - r - 1, rest)
+    p[len(placed):, 2] = rng.uniform(r + 1, cfg.lz - r - 1, rest)
+    f, g, f7 = W.initial_state(cfg)
+    s.load_state(f, g, f7, p)
+    o.load_state(f, g, f7, p)
+    assert np.array_equal(s.flags(), o.flags())
+    if storage == 0:
+        _links_equal(s, o)
+    else:
+        a, b = s.links(), o.links()
+        assert len(a[0]) == len(b[0])
+        for x, y in zip(a[:3], b[:3]):
+            assert np.array_equal(x, y)
+        # q in FP32 away from its decision edges: the cancellation in -b - sqrt(disc) leaves a few
+        # 1e-6 (3.2e-6 measured)
+        np.testing.assert_allclose(a[3], b[3], rtol=0, atol=1e-5)
 
 
 def test_links_contacts_new_fluid_bit_exact_at_identical_state(env):
