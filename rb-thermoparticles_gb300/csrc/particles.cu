@@ -921,8 +921,8 @@ __global__ void __launch_bounds__(NT) k_mark(const Geo geo, const Phys ph, const
 // and a bit select in its node's mask, the ray-sphere q of links.cu:7-23 runs with all lanes busy,
 // and candidate k goes to slab entry base + k, so the slab holds the links in the reference's
 // (idx, ip) order (links.cu:221-250).  A candidate whose ray-sphere test fails (a grazing ray
-// rounded off the sphere) is rare; a block vote finds the groups that hold one, and only those
-// are compacted by a block scan.  Only the spherical shell that can hold link nodes is
+// rounded off the sphere) is rare; one block vote per chunk finds the chunks that hold one, and
+// only those are redone with an order-preserving compaction (block scans).  Only the spherical shell that can hold link nodes is
 // enumerated: per (y, z) row of the box, the x-intervals between an inner radius (nodes inside it
 // are certainly solid) and the outer reach r + 2, with float margins so that every possible link
 // node is kept; rows are numbered by a block scan and flat indices are mapped back by a binary
@@ -1022,56 +1022,62 @@ __device__ __forceinline__ void link_fill_body(const Geo &geo, const Phys &ph, c
         sm.scan[threadIdx.x] = pos;
         sm.node[threadIdx.x] = my_node;
         __syncthreads();
-        // phase 2: q for the numbered candidates, order-preserving append
-        for (int k0 = 0; k0 < ccount; k0 += NT) {
-            const int k = k0 + threadIdx.x;
-            int ok = 0, node = 0, dw = 0;
+        // phase 2: q for the numbered candidates.  Candidate k is written to slab entry base + k;
+        // a chunk holding a ray that failed the ray-sphere test (rare: a grazing ray rounded off
+        // the surface) is redone with an order-preserving compaction.
+        auto candidate = [&](int k, int &node, int &dw, double &q) -> bool {
+            // the chunk thread j holding candidate k: the last j with scan[j] <= k
+            int lo = 0, hi = NT - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (sm.scan[mid] <= k) lo = mid;
+                else hi = mid - 1;
+            }
+            const int ip = (int)__fns(sm.mask[lo], 0u, k - sm.scan[lo] + 1);
+            node = sm.node[lo];
+            dw = ip | (int)(((sm.up[lo] >> dopp_rt(ip)) & 1u) << LINK_UP);
+            const int iz = node / lxy;
+            const int iy = (node - iz * lxy) / lx;
+            const int ix = node - iz * lxy - iy * lx;
+            int r32 = -1;
+            if constexpr (F32Q)
+                r32 = link_q_f32(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (float)(ix - ipx) + hx,
+                                 (float)(iy - ipy) + hy, (float)(iz - ipz) + hz, pg.rf2, q);
+            if (r32 > 0) return true;
+            const double *st = pb.state;
+            return link_q(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (double)ix + 0.5, (double)iy + 0.5,
+                          (double)iz + 0.5, PCOL(st, pb.np, 0, p), PCOL(st, pb.np, 1, p),
+                          PCOL(st, pb.np, 2, p), dmul(ph.radius, ph.radius), q);
+        };
+        auto put = [&](int pos, int node, int dw, double q) {
+            if (pos < pb.link_cap) {
+                pb.link_node[slab + pos] = node;
+                pb.link_dir[slab + pos] = dw;
+                pb.link_q[slab + pos] = q;
+            }
+        };
+        int rejected = 0;
+        for (int k = threadIdx.x; k < ccount; k += NT) {
+            int node, dw;
             double q = 0.0;
-            if (k < ccount) {
-                // the chunk thread j holding candidate k: the last j with scan[j] <= k
-                int lo = 0, hi = NT - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (sm.scan[mid] <= k) lo = mid;
-                    else hi = mid - 1;
-                }
-                const int ip = (int)__fns(sm.mask[lo], 0u, k - sm.scan[lo] + 1);
-                node = sm.node[lo];
-                dw = ip | (int)(((sm.up[lo] >> dopp_rt(ip)) & 1u) << LINK_UP);
-                const int iz = node / lxy;
-                const int iy = (node - iz * lxy) / lx;
-                const int ix = node - iz * lxy - iy * lx;
-                int r32 = -1;
-                if constexpr (F32Q)
-                    r32 = link_q_f32(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (float)(ix - ipx) + hx,
-                                     (float)(iy - ipy) + hy, (float)(iz - ipz) + hz, pg.rf2, q);
-                if (r32 > 0) {
-                    ok = 1;
-                } else {
-                    const double *st = pb.state;
-                    ok = link_q(dcx_rt(ip), dcy_rt(ip), dcz_rt(ip), (double)ix + 0.5, (double)iy + 0.5,
-                                (double)iz + 0.5, PCOL(st, pb.np, 0, p), PCOL(st, pb.np, 1, p),
-                                PCOL(st, pb.np, 2, p), dmul(ph.radius, ph.radius), q) ? 1 : 0;
-                }
-            }
-            int lpos, ltotal;
-            if (__syncthreads_or(k < ccount && !ok)) {
-                lpos = base + block_exclusive_scan<NT>(ok, sm.rows.wsum, ltotal);
-            } else {
-                lpos = base + threadIdx.x;   // every candidate of the group is a link
-                ltotal = min(NT, ccount - k0);
-            }
-            if (ok) {
-                if (lpos < pb.link_cap) {
-                    pb.link_node[slab + lpos] = node;
-                    pb.link_dir[slab + lpos] = dw;
-                    pb.link_q[slab + lpos] = q;
-                } else {
-                    atomicOr(&status->link_overflow, 1);
-                }
-            }
-            base += ltotal;
+            if (candidate(k, node, dw, q)) put(base + k, node, dw, q);
+            else rejected = 1;
         }
+        if (__syncthreads_or(rejected)) {
+            for (int k0 = 0; k0 < ccount; k0 += NT) {
+                const int k = k0 + threadIdx.x;
+                int node = 0, dw = 0, ok = 0;
+                double q = 0.0;
+                if (k < ccount) ok = candidate(k, node, dw, q) ? 1 : 0;
+                int ltotal;
+                const int lpos = base + block_exclusive_scan<NT>(ok, sm.rows.wsum, ltotal);
+                if (ok) put(lpos, node, dw, q);
+                base += ltotal;
+            }
+        } else {
+            base += ccount;
+        }
+        if (base > pb.link_cap && threadIdx.x == 0) atomicOr(&status->link_overflow, 1);
         __syncthreads();
     }
     if (threadIdx.x == 0) pb.link_cnt[p] = base;
