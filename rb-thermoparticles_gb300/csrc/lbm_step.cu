@@ -36,6 +36,8 @@ template <int MODE, bool PULL, int OUT>
 __global__ void __launch_bounds__(128, MODE == RBTP_STORE_F64 ? RBTP_STEP_MINB_F64 : RBTP_STEP_MINB_LOW)
     k_step(const Geo geo, const Phys ph, const StepBuffers b)
 {
+    pdl_wait();
+    pdl_trigger();
     const int ix = blockIdx.x * blockDim.x + threadIdx.x;
     const int iy = blockIdx.y * blockDim.y + threadIdx.y;
     const int iz = blockIdx.z;
@@ -201,10 +203,7 @@ cudaError_t launch_step_mode(bool pull, int out, const Geo &geo, const Phys &ph,
     const dim3 blk = MODE == RBTP_STORE_F16S ? dim3(16, 8, 1) : dim3(32, 4, 1);
     const dim3 grd = node_grid(geo, blk);
 #define RBTP_STEP_CASE(P, O)                                                       \
-    if (pull == P && out == O) {                                                   \
-        k_step<MODE, P, O><<<grd, blk, 0, st>>>(geo, ph, b);                       \
-        return cudaGetLastError();                                                 \
-    }
+    if (pull == P && out == O) return pdl_launch(k_step<MODE, P, O>, grd, blk, st, geo, ph, b);
     RBTP_STEP_CASE(true, OUT_NONE)
     RBTP_STEP_CASE(true, OUT_RHO)
     RBTP_STEP_CASE(true, OUT_MACROS)
