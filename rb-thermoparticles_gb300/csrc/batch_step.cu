@@ -56,12 +56,12 @@ __global__ void k_batch_advance(CavDesc *desc, int n)
 }
 
 template <int MODE, bool PULL>
-__device__ __forceinline__ void step_out(const CavDesc &d, const StepBuffers &b, int out, int ix, int iy,
-                                         int iz)
+__device__ __forceinline__ void step_out(const Geo &geo, const Phys &ph, const StepBuffers &b, int out, int ix,
+                                         int iy, int iz)
 {
-    if (out == OUT_NONE) step_node<MODE, PULL, OUT_NONE, false>(d.geo, d.ph, b, ix, iy, iz);
-    else if (out == OUT_RHO) step_node<MODE, PULL, OUT_RHO, false>(d.geo, d.ph, b, ix, iy, iz);
-    else step_node<MODE, PULL, OUT_MACROS, false>(d.geo, d.ph, b, ix, iy, iz);
+    if (out == OUT_NONE) step_node<MODE, PULL, OUT_NONE, false>(geo, ph, b, ix, iy, iz);
+    else if (out == OUT_RHO) step_node<MODE, PULL, OUT_RHO, false>(geo, ph, b, ix, iy, iz);
+    else step_node<MODE, PULL, OUT_MACROS, false>(geo, ph, b, ix, iy, iz);
 }
 
 // The batched kernel carries all phase/output variants of the step body behind block-uniform
@@ -77,11 +77,23 @@ __global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MI
 {
     pdl_wait();
     pdl_trigger();
+    // the member's lattice and relaxation constants, staged per tile in shared memory (the step body
+    // reads them many times; the single-cavity kernel has them as launch parameters)
+    __shared__ Geo sgeo;
+    __shared__ Phys sph;
+    constexpr int GW = sizeof(Geo) / 4, PW = sizeof(Phys) / 4;
+    const int tid = threadIdx.y * TX + threadIdx.x;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 tl = tiles[t];
         const CavDesc &d = desc[tl.x];
+        __syncthreads();   // the previous tile's readers are done
+        for (int k = tid; k < GW + PW; k += TX * TY) {
+            if (k < GW) reinterpret_cast<int *>(&sgeo)[k] = reinterpret_cast<const int *>(&d.geo)[k];
+            else reinterpret_cast<int *>(&sph)[k - GW] = reinterpret_cast<const int *>(&d.ph)[k - GW];
+        }
+        __syncthreads();
         const int ix = tl.y * TX + threadIdx.x, iy = tl.z * TY + threadIdx.y, iz = tl.w;
-        if (d.out == OUT_IDLE || ix >= d.geo.lx || iy >= d.geo.ly) continue;
+        if (d.out == OUT_IDLE || ix >= sgeo.lx || iy >= sgeo.ly) continue;
         const int cur = d.cur;
         StepBuffers b;
         b.fin = d.f[cur];
@@ -93,8 +105,8 @@ __global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MI
         b.rho = d.rho; b.ux = d.ux; b.uy = d.uy; b.uz = d.uz; b.phi = d.phi;
         b.fcol = nullptr; b.gcol = nullptr;
         b.status = d.status;
-        if (d.phase) step_out<MODE, true>(d, b, d.out, ix, iy, iz);
-        else step_out<MODE, false>(d, b, d.out, ix, iy, iz);
+        if (d.phase) step_out<MODE, true>(sgeo, sph, b, d.out, ix, iy, iz);
+        else step_out<MODE, false>(sgeo, sph, b, d.out, ix, iy, iz);
     }
 }
 
