@@ -168,3 +168,25 @@ def test_reference_pin_particles(driver, oracle_mod, tmp_path):
         node, d, pid, q = impl.links()
         assert np.array_equal(node, rn) and np.array_equal(d, rd) and np.array_equal(pid, rp)
         assert np.abs(q - rq).max() < 1e-10
+
+
+@pytest.mark.parametrize("case", ["ref_single", "ref_particles"])
+def test_librbtp_against_reference_golden_fixtures(lib_built, oracle_mod, case):
+    """librbtp from the same inputs as tests/golden/make_golden.py reproduces the fixtures the
+    reference's kernels produced (the pin without the reference's cubins: runs everywhere)."""
+    sys.path.insert(0, os.path.join(REPO, "tests", "golden"))
+    import make_golden as MG
+    from test_oracle_golden import check_against_golden
+    data = dict(np.load(os.path.join(REPO, "tests", "golden", case + ".npz")))
+    cfg, f, g, f7, parts = MG.inputs(case, oracle_mod)
+    s = Solver(cfg)
+    s.load_state(f, g, f7, parts)
+    if parts is not None:
+        npart = len(parts)
+        assert np.array_equal(MG.solid_counts(s.flags(), npart), data["solid0"])
+        node, d, pid, q = s.links()
+        got = MG.link_checksums(node, d, pid, q, npart)
+        assert np.array_equal(got[:, :3], data["links0"][:, :3])
+        assert np.all(np.abs(got[:, 3] - data["links0"][:, 3]) <= 1e-12 * np.maximum(data["links0"][:, 0], 1))
+    s.step(MG.STEPS, macros_last=True)
+    check_against_golden(s, case, data)
