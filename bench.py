@@ -505,7 +505,7 @@ def run_ours(args) -> dict:
         "data": "synthetic: seeded linear-conduction start (SplitMix64 +-1e-3 perturbation)",
         "config": {"workload": "production single-phase RB 320x320x160, Ra=1e8, Pr=0.71, FP32-store",
                    "nodes": head["nodes"], "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                   "l2": "state (7.3 GB) exceeds L2; no flush needed"},
+                   "l2": "state (7.2 GB) exceeds L2; no flush needed"},
         "roofline": head["roofline"],
         "clocks": clocks,
         "gpu_launches": head["launches_per_step"] * args.steps,
@@ -576,8 +576,10 @@ def run_reference(args) -> dict | None:
     return {"metric": "MLUPS (lattice-node updates/s), 320x320x160 D3Q27 f+g RB step, FP32-store",
             "value": round(v, 3), "unit": "MLUPS", "impl": "reference", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
-            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "production single-phase RB 320x320x160, Ra=1e8, Pr=0.71 (slab sample)"},
+            "higher_is_better": True, "scaling": "weak", "dtype": "f64", "data": "synthetic",
+            # the same workload as the default arm, timed on a bounded slab sample (cpu_baseline.sample)
+            "config": {"workload": "production single-phase RB 320x320x160, Ra=1e8, Pr=0.71, FP32-store",
+                       "nodes": 320 * 320 * 160, "parallelism": "host cores"},
             "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
