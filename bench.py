@@ -28,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 REPO = os.path.dirname(os.path.abspath(__file__))
@@ -72,8 +73,9 @@ class ClockSampler:
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
-        self.path = os.path.join(REPO, "gpurun_out" if os.path.isdir(os.path.join(REPO, "gpurun_out")) else "_work",
-                                 f"clocks_{os.getpid()}.csv")
+        # raw samples: $RBTP_CLOCKS_DIR if set (to keep them), else the system temporary directory
+        self.path = os.path.join(os.environ.get("RBTP_CLOCKS_DIR") or tempfile.gettempdir(),
+                                 f"rbtp_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:

@@ -141,8 +141,9 @@ int  rbtp_load_restart(rbtp_handle *h, const char *dir, int step);
 
 /* ---- time stepping ------------------------------------------------------------------------- */
 /* Advance nsteps full steps in main.cu:35-84 order (macrovar → forcing → collide/stream f →
- * IBB f → collide/stream g → IBB g → contacts → forces/heat → move → links → refill), fused as
- * described in the design doc.  Macroscopic fields are materialised on steps that hit the config's
+ * IBB f → collide/stream g → IBB g → contacts → forces/heat → move → links → refill), fused into
+ * one pull-stream/collide kernel per step plus the particle kernels.  Macroscopic fields are
+ * materialised on steps that hit the config's
  * output cadence (NDIAG, NNUOUT, NFLOWOUT, NEND) and, with RBTP_STEP_MACROS_LAST, on the last
  * step of the call. */
 #define RBTP_STEP_MACROS_LAST 1u
