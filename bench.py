@@ -41,7 +41,7 @@ FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_step launch on the
 # 320x320x160 single-phase workload, from a one-pass ncu capture of
 # `python bench.py --only production:<storage> --steps 3 --warmup 3`
-# (profiles/k_step_dram_320x320x160.md).  Algorithmic bytes per launch: 16,384,000 nodes x
+# (the capture's summary is kept with the other ncu summaries).  Algorithmic bytes per launch: 16,384,000 nodes x
 # bytes_per_node.
 NCU_DRAM_BYTES = {"f64": 7.30e9 + 7.16e9, "f32": 3.62e9 + 3.63e9, "f16s": 1.84e9 + 1.80e9}
 
