@@ -577,7 +577,6 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
             // slabs stay on the main stream: beside the HBM-bound bulk kernel their CTAs would take
             // its SM slots (measured slower).
             int *oc = h->owner[h->ocur], *on = h->owner[1 - h->ocur];
-            h->pb.owner_cur = oc;
             CK(cudaEventRecord(h->ev_fork, h->stream));
             CK(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
             CK(launch_contacts(h->geo, h->ph, h->pb, h->status, h->side));
@@ -590,7 +589,6 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
             CK(launch_refill(h->mode, h->geo, h->ph, h->pb, oc, on, h->f[dst], h->g[dst], h->faux,
                              h->rho_wall, macro, h->rho, h->ux, h->uy, h->uz, h->phi, h->status, h->stream));
             h->ocur = 1 - h->ocur;
-            h->pb.owner_cur = h->owner[h->ocur];
         }
         h->cur = dst;
         h->phase = PHASE_COLLIDED;
@@ -1245,7 +1243,6 @@ int rbtp_checkpoint_read(rbtp_handle *h, const char *path)
         s = build_links(h, h->owner[0]);
         if (s) return s;
     }
-    h->pb.owner_cur = h->owner[0];
     CK(cudaStreamSynchronize(h->stream));   // host staging buffers go out of scope
     h->istep = hd.istep;
     h->initialised = true;

@@ -242,7 +242,6 @@ int sync_back(rbtp_batch *b)
         h->ocur = d.ocur;
         h->phase = d.phase ? PHASE_COLLIDED : PHASE_HOME;
         h->istep = d.istep;
-        h->pb.owner_cur = h->owner[h->ocur];
         h->macros_valid = d.last_out == OUT_MACROS;
         h->dissip_valid = false;
         h->plane_valid = false;

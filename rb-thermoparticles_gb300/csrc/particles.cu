@@ -1374,12 +1374,6 @@ cudaError_t launch_mark(const Geo &geo, const Phys &ph, const PartBuffers &pb, i
     return cudaGetLastError();
 }
 
-cudaError_t launch_initial_owner(const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                                 int *owner, cudaStream_t st)
-{
-    return launch_mark(geo, ph, pb, owner, st);
-}
-
 cudaError_t launch_link_fill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
                              const int *owner, DevStatus *status, cudaStream_t st)
 {

@@ -339,7 +339,6 @@ struct PartBuffers {
     int ibb_chunks;         // link chunks (CTAs) per particle, 1..IBB_CHUNKS, from the link capacity
     PGeo *pgeo;             // np entries, refreshed before every marking pass
     double *cF;             // contact force (3*np)
-    int *owner_cur, *owner_new;   // solid owner maps (L each); -1 = fluid
     int link_cap;           // links per particle slab
     int *link_node, *link_cnt;
     int *link_dir;          // direction ip in bits 0-4, LINK_UP set when x - c_ip is in-domain fluid
@@ -372,8 +371,6 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
                           void *faux, const double *rho_wall, bool macros, double *rho,
                           double *ux, double *uy, double *uz, double *phi, DevStatus *status,
                           cudaStream_t st);
-cudaError_t launch_initial_owner(const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                                 int *owner, cudaStream_t st);
 
 // ------------------------------------------------------------------------------------------------
 // Batched execution: one descriptor per cavity in device memory.  The step state (buffer parity,
