@@ -71,3 +71,17 @@ def test_workload_configs():
     assert p.lx == 320 and p.rho_particle_ratio == 1.5
     if d is not None:
         assert d.npart == 1000 and d.particle_radius == 8.0
+
+
+def test_footprint_covers_the_population_buffers(lib_built):
+    """rbtp_footprint (the server's admission size) is host arithmetic: for every storage mode it
+    covers the two population buffers (27 L paired (f, g) slots each, FP64 keeps separate f and g
+    arrays), orders the modes by their bytes, and grows with particles."""
+    from rbtp import footprint
+    L = 320 * 320 * 160
+    pop = {0: 2 * 2 * 27 * L * 8, 1: 2 * 27 * L * 8, 2: 2 * 27 * L * 4}
+    fp = {st: footprint(W.config("production", storage=st)) for st in (0, 1, 2)}
+    for st in (0, 1, 2):
+        assert pop[st] <= fp[st] < pop[st] + 16 * 8 * L     # plus at most 16 FP64 fields per node
+    assert fp[0] > fp[1] > fp[2]
+    assert footprint(W.config("particle_laden", storage=1)) > fp[1]
