@@ -109,9 +109,9 @@ cudaError_t aux_from_host(rbtp_handle *h, const double *src)
 
 // Build the current solid flags and the IBB link slabs from the current particle positions
 // (build_links, links.cu:572-685).
-int build_links(rbtp_handle *h, int *owner)
+int build_links(rbtp_handle *h, int *owner, bool pgeo_fresh = false)
 {
-    CK(launch_mark(h->geo, h->ph, h->pb, owner, h->stream));
+    CK(launch_mark(h->geo, h->ph, h->pb, owner, h->stream, !pgeo_fresh));
     CK(launch_link_fill(h->mode, h->geo, h->ph, h->pb, owner, h->status, h->stream));
     return RBTP_OK;
 }
@@ -583,8 +583,8 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
             CK(cudaEventRecord(h->ev_side, h->side));
             CK(launch_links_ibb(h->mode, h->geo, h->ph, h->pb, h->f[dst], h->g[dst], h->rho, h->stream));
             CK(cudaStreamWaitEvent(h->stream, h->ev_side, 0));
-            CK(launch_update(h->ph, h->pb, h->stream));
-            s = build_links(h, on);
+            CK(launch_update(h->geo, h->ph, h->pb, h->stream));   // also refreshes the geometry cache
+            s = build_links(h, on, true);
             if (s) return s;
             CK(launch_refill(h->mode, h->geo, h->ph, h->pb, oc, on, h->f[dst], h->g[dst], h->faux,
                              h->rho_wall, macro, h->rho, h->ux, h->uy, h->uz, h->phi, h->status, h->stream));

@@ -861,10 +861,15 @@ __device__ __forceinline__ void update_body(const Phys &ph, const PartBuffers &p
     for (int c = 0; c < 33; ++c) PCOL(st, np, c, p) = out[c];
 }
 
-__global__ void k_update(const Phys ph, const PartBuffers pb)
+// The integrator, followed by the geometry cache of the new position (same thread, same particle),
+// so the link build that follows needs no separate k_pgeo launch.
+__global__ void k_update(const Geo geo, const Phys ph, const PartBuffers pb)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < pb.np) update_body(ph, pb, p);
+    if (p < pb.np) {
+        update_body(ph, pb, p);
+        pgeo_body(geo, ph, pb, p);
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1355,20 +1360,20 @@ cudaError_t launch_contacts(const Geo &geo, const Phys &ph, const PartBuffers &p
     return cudaGetLastError();
 }
 
-cudaError_t launch_update(const Phys &ph, const PartBuffers &pb, cudaStream_t st)
+cudaError_t launch_update(const Geo &geo, const Phys &ph, const PartBuffers &pb, cudaStream_t st)
 {
     if (pb.np <= 0) return cudaSuccess;
-    k_update<<<(pb.np + 127) / 128, 128, 0, st>>>(ph, pb);
+    k_update<<<(pb.np + 127) / 128, 128, 0, st>>>(geo, ph, pb);
     return cudaGetLastError();
 }
 
 cudaError_t launch_mark(const Geo &geo, const Phys &ph, const PartBuffers &pb, int *owner_out,
-                        cudaStream_t st)
+                        cudaStream_t st, bool pgeo)
 {
     cudaError_t e = cudaMemsetAsync(owner_out, 0xFF, sizeof(int) * (size_t)geo.L, st);
     if (e) return e;
     if (pb.np <= 0) return cudaSuccess;
-    k_pgeo<<<(pb.np + 127) / 128, 128, 0, st>>>(geo, ph, pb);
+    if (pgeo) k_pgeo<<<(pb.np + 127) / 128, 128, 0, st>>>(geo, ph, pb);
     if (pb.np < PARTICLES_WIDE) k_mark<LINK_WIDE><<<pb.np, LINK_WIDE, 0, st>>>(geo, ph, pb, owner_out);
     else k_mark<LINK_NARROW><<<pb.np, LINK_NARROW, 0, st>>>(geo, ph, pb, owner_out);
     return cudaGetLastError();
@@ -1501,6 +1506,7 @@ __global__ void k_update_b(const CavDesc *desc, const int2 *pmap, int total)
     const CavDesc &d = desc[mp.x];
     if (d.out == OUT_IDLE) return;
     update_body(d.ph, d.pb, mp.y);
+    pgeo_body(d.geo, d.ph, d.pb, mp.y);   // geometry cache of the new position
 }
 
 __global__ void k_owner_fill_b(const CavDesc *desc, const int *pmem)
@@ -1513,18 +1519,6 @@ __global__ void k_owner_fill_b(const CavDesc *desc, const int *pmem)
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < d.geo.L;
          i += (long long)gridDim.x * blockDim.x)
         o[i] = -1;
-}
-
-__global__ void k_pgeo_b(const CavDesc *desc, const int2 *pmap, int total)
-{
-    pdl_wait();
-    pdl_trigger();
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= total) return;
-    const int2 mp = pmap[g];
-    const CavDesc &d = desc[mp.x];
-    if (d.out == OUT_IDLE) return;
-    pgeo_body(d.geo, d.ph, d.pb, mp.y);
 }
 
 template <int NT>
@@ -1617,7 +1611,6 @@ cudaError_t particles_batched_mode(const CavDesc *desc, const int2 *pmap, int to
     if ((e = cudaStreamWaitEvent(st, ev_join, 0)) != cudaSuccess) return e;
     RBTP_PDL(k_update_b, dim3(bl), dim3(t), st, desc, pmap, total);
     RBTP_PDL(k_owner_fill_b, dim3(64, npmem), dim3(256), st, desc, pmem);
-    RBTP_PDL(k_pgeo_b, dim3(bl), dim3(t), st, desc, pmap, total);
     if (total < PARTICLES_WIDE) {
         RBTP_PDL(k_mark_b<LINK_WIDE>, dim3(total), dim3(LINK_WIDE), st, desc, pmap);
         RBTP_PDL(k_link_fill_b<MODE != RBTP_STORE_F64, LINK_WIDE>, dim3(total), dim3(LINK_WIDE), st, desc, pmap);

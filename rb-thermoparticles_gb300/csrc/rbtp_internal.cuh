@@ -361,9 +361,11 @@ cudaError_t launch_links_ibb(int mode, const Geo &geo, const Phys &ph, const Par
                              void *f, void *g, const double *rho, cudaStream_t st);
 cudaError_t launch_contacts(const Geo &geo, const Phys &ph, const PartBuffers &pb,
                             DevStatus *status, cudaStream_t st);
-cudaError_t launch_update(const Phys &ph, const PartBuffers &pb, cudaStream_t st);
+// The integrator also refreshes the particles' geometry cache (PGeo) for their new positions.
+cudaError_t launch_update(const Geo &geo, const Phys &ph, const PartBuffers &pb, cudaStream_t st);
+// pgeo: refresh the geometry cache first (false right after launch_update, which did it)
 cudaError_t launch_mark(const Geo &geo, const Phys &ph, const PartBuffers &pb, int *owner_out,
-                        cudaStream_t st);
+                        cudaStream_t st, bool pgeo = true);
 cudaError_t launch_link_fill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
                              const int *owner, DevStatus *status, cudaStream_t st);
 cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
