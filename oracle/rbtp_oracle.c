@@ -397,7 +397,7 @@ static int ensure_links(orc_sim *s, int n)
     return 0;
 }
 
-/* links.cu:572-685 (build_links): per-particle marking in pid order, where the first marker of a
+/* links.cu:143-256 (build_links): per-particle marking in pid order, where the first marker of a
  * node keeps it (links.cu:45), then link count, exclusive scan and fill in node order. */
 static int o_build_links(orc_sim *s)
 {

@@ -1,8 +1,9 @@
 #!/usr/bin/env python3
 """Compile the reference's own device code, per pin case, into oracle/_ref/<case>.cubin.
 
-TEST INFRASTRUCTURE ONLY.  Reads the reference sources where they lie (/root/reference, present only
-on the development machine), compiles them with nvcc for sm_103a (-rdc, the reference's
+TEST INFRASTRUCTURE ONLY.  Reads the reference sources where they lie (the directory given by
+--reference, else $RBTP_REFERENCE_DIR, else /root/reference; present only on the development
+machine), compiles them with nvcc for sm_103a (-rdc, the reference's
 -std=c++14 raised to c++17 because CUDA 13's headers require it) against a generated parameters.h,
 and device-links the objects into one cubin.  Nothing is copied from the reference: outputs go to
 oracle/_ref/ only (git-ignored), and the cubin travels to GPU hosts as a build artefact.  The host
@@ -17,7 +18,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 import cases  # noqa: E402
 
-REF = "/root/reference"
+DEFAULT_REF = "/root/reference"
+REF = os.environ.get("RBTP_REFERENCE_DIR") or DEFAULT_REF
+
+
+def reference_dir() -> str:
+    """The reference source tree this recipe reads (see the module docstring)."""
+    return REF
 OUT = os.path.join(os.path.dirname(HERE), "_ref")
 # main.cu and output/*.cu launch macrovar/collision/streaming and compute_Ked/ted; compiling them
 # keeps those kernels referenced so the device link does not discard them.
@@ -63,6 +70,14 @@ def build_case(case: str) -> str:
 
 
 def main() -> int:
+    global REF
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=None, help="reference source tree (default: $RBTP_REFERENCE_DIR "
+                    "or " + DEFAULT_REF + ")")
+    a = ap.parse_args()
+    if a.reference:
+        REF = a.reference
     if not os.path.isdir(REF):
         print("reference sources not present; nothing to build")
         return 0

@@ -12,6 +12,11 @@ CASES = {
                        visc=0.1414 * 32 * math.sqrt(0.71 / 1.0e6), activate_particles=0,
                        particle_fraction=0.0, particle_diam_frac=1.0 / 20.0,
                        rho_particle_ratio=1.0),
+    # the plain FP64 parity configuration: 64x64x32, Ra = 1e6, single phase
+    "ref_config1": dict(lx=64, ly=64, lz=32, rayleigh=1.0e6, prandtl=0.71,
+                        visc=0.1414 * 64 * math.sqrt(0.71 / 1.0e6), activate_particles=0,
+                        particle_fraction=0.0, particle_diam_frac=1.0 / 20.0,
+                        rho_particle_ratio=1.0),
     # nine spheres of diameter 8 in 48x48x24
     "ref_particles": dict(lx=48, ly=48, lz=24, rayleigh=1.0e6, prandtl=0.71,
                           visc=0.1414 * 48 * math.sqrt(0.71 / 1.0e6), activate_particles=1,
@@ -41,9 +46,13 @@ FIXED = dict(continuous_steps=0, nend=1000000, ndiag=125, nflowout=25000, nnuout
              rep_stf1_w=0.002)
 
 
-def values(case: str) -> dict:
+def values(case: str, **over) -> dict:
+    """parameters.h values of a case.  Overrides may change what the compiled kernels take at run
+    time (Ra, Pr and VISC enter only through the constants the driver sets; the density ratio only
+    through the particle mass and the integrator's argument), not the compiled sizes."""
     v = dict(FIXED)
     v.update(CASES[case] if case in CASES else TIMING[case])
+    v.update(over)
     return v
 
 

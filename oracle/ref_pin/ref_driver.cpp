@@ -3,7 +3,7 @@
 // and librbtp against the reference's device arithmetic on the same GPU.
 //
 // TEST INFRASTRUCTURE ONLY.  The host sequence follows main.cu:32-85 and the wrappers
-// build_links (links.cu:572-685), bounce_back_* / compute_particle_* (ibb.cu:209-271),
+// build_links (links.cu:143-256), bounce_back_* / compute_particle_* (ibb.cu:209-271),
 // prepare_particle_forces_step / apply_repulsive_forces (pforces.cu:80-148),
 // update_particles (move.cu:107-142), refill_nodes (refill.cu:244-329) and the restart load of
 // initial.cu:194-236.  CUB's device scans are replaced by host integer scans (same results).
@@ -12,6 +12,16 @@
 //   in_dir:  cfg.txt (key value lines), f.bin, g.bin, flow7.bin, particles.bin (np x 33, optional)
 //   out_dir: links0.bin owner0.bin (loaded state), f.bin g.bin macros.bin particles.bin owner.bin
 //            links.bin newfluid.bin (after nsteps)
+//
+//   With "sample_stride k" (k > 1) in cfg.txt, f.bin, g.bin and macros.bin hold every k-th node only
+//   (node indices 0, k, 2k, ...; each direction or field in turn) and fgnorm.bin holds, per direction,
+//   sum f_i, sum f_i^2, sum g_i, sum g_i^2 over all nodes: full-size cases without 7 GB dumps.
+//
+// Nu series: ref_driver <cubin> <in_dir> nu <nsteps> <every> <out_file>
+//   Runs nsteps steps and after every `every`-th step appends the Nu row of output_nu
+//   (output_statis.cu:111-223: step, volume fraction, Nu_bulk, Nu_top, Nu_bottom, Nu_bulk_fluid,
+//   Nu_bulk_part; 7 doubles) computed on the host from the reference kernels' d_ux, d_phi and
+//   d_ibnode of that step.
 //
 // timing: ref_driver <cubin> <in_dir> time <warmup> <steps>
 //   Times the reference's per-step sequence (kernels and device-to-device copies exactly as its host
@@ -156,7 +166,7 @@ void host_scan(int n_total_last, int &total)
     (void)n_total_last;
 }
 
-// links.cu:572-685
+// links.cu:143-256
 void build_links()
 {
     std::vector<double> px(NP), py(NP), pz(NP);
@@ -329,16 +339,85 @@ void synthetic_state(std::vector<char> &f, std::vector<char> &g, std::vector<cha
     }
 }
 
+// The Nu row of output_nu (output_statis.cu:111-223) from the device's d_ux, d_phi and (with
+// particles) d_ibnode as they stand after a step: plane-averaged u_x T over fluid and solid nodes,
+// and the wall gradients (T_hot - T(x = 1/2)) / (1/2) and (T(LX - 1/2) - T_cold) / (1/2) over fluid
+// wall nodes, scaled as that function scales them.
+void nu_row(int istep, double *row)
+{
+    std::vector<double> ux(L), phi(L);
+    std::vector<int> ib(NP > 0 ? L : 0);
+    CU(cuMemcpyDtoH(ux.data(), d_ux, L * sizeof(double)));
+    CU(cuMemcpyDtoH(phi.data(), d_phi, L * sizeof(double)));
+    if (NP > 0) CU(cuMemcpyDtoH(ib.data(), d_ibnode, L * sizeof(int)));
+    const double th = cfg["t_hot"], tc = cfg["t_cold"], diff = cfg["diff"];
+    const double vf = cfg.count("particle_fraction") ? cfg["particle_fraction"] : 0.0;
+    const double cp = cfg.count("cp_particle_ratio") ? cfg["cp_particle_ratio"] : 0.0;
+    const double fluid_frac = std::fmax(0.0, 1.0 - vf);
+    const long long lxy = (long long)LX * LY;
+    auto solid = [&](long long n) { return NP > 0 && ib[n] != 0; };
+    double avg_f = 0.0, avg_p = 0.0;
+    for (int ix = 0; ix < LX; ++ix) {
+        double sf = 0.0, sp = 0.0;
+        long long nf = 0, npart = 0;
+        for (int iz = 0; iz < LZ; ++iz)
+            for (int iy = 0; iy < LY; ++iy) {
+                const long long n = iz * lxy + (long long)iy * LX + ix;
+                if (solid(n)) { sp += ux[n] * phi[n]; ++npart; }
+                else { sf += ux[n] * phi[n]; ++nf; }
+            }
+        if (nf > 0) avg_f += sf / (double)nf;
+        if (npart > 0) avg_p += sp / (double)npart;
+    }
+    avg_f /= (double)LX;
+    avg_p /= (double)LX;
+    const double cond = diff * (th - tc) / (double)LX;
+    double nb_fluid = fluid_frac, nb_part = 0.0;
+    if (cond != 0.0) {
+        nb_fluid += fluid_frac * (avg_f / cond);
+        nb_part = vf * cp * (avg_p / cond);
+    }
+    double bot = 0.0, top = 0.0;
+    long long nb = 0, nt = 0;
+    for (int iz = 0; iz < LZ; ++iz)
+        for (int iy = 0; iy < LY; ++iy) {
+            const long long n0 = iz * lxy + (long long)iy * LX, n1 = n0 + LX - 1;
+            if (!solid(n0)) { bot += (th - phi[n0]) / 0.5; ++nb; }
+            if (!solid(n1)) { top += (phi[n1] - tc) / 0.5; ++nt; }
+        }
+    const double area = (double)LY * (double)LZ, scale = (double)LX / (th - tc);
+    row[0] = (double)istep;
+    row[1] = vf;
+    row[2] = nb_fluid + nb_part;
+    row[3] = nt > 0 ? (top / area) * scale : 0.0;
+    row[4] = nb > 0 ? (bot / area) * scale : 0.0;
+    row[5] = nb_fluid;
+    row[6] = nb_part;
+}
+
+// Every stride-th node of a device array of n fields of L doubles, field after field.
+std::vector<double> sampled(CUdeviceptr d, int nfield, long long stride)
+{
+    std::vector<double> plane(L), out;
+    for (int k = 0; k < nfield; ++k) {
+        CU(cuMemcpyDtoH(plane.data(), d + (size_t)k * L * 8, L * 8));
+        for (long long n = 0; n < L; n += stride) out.push_back(plane[n]);
+    }
+    return out;
+}
+
 int run(int argc, char **argv)
 {
     const bool timing = argc == 6 && std::string(argv[3]) == "time";
-    if (argc != 5 && !timing) {
+    const bool nu_mode = argc == 7 && std::string(argv[3]) == "nu";
+    if (argc != 5 && !timing && !nu_mode) {
         std::fprintf(stderr, "usage: ref_driver <cubin> <in_dir> <nsteps> <out_dir>\n"
+                             "       ref_driver <cubin> <in_dir> nu <nsteps> <every> <out_file>\n"
                              "       ref_driver <cubin> <in_dir> time <warmup> <steps>\n");
         return 2;
     }
-    const std::string in = argv[2], out = timing ? std::string() : std::string(argv[4]);
-    const int nsteps = timing ? 0 : std::atoi(argv[3]);
+    const std::string in = argv[2], out = (timing || nu_mode) ? std::string() : std::string(argv[4]);
+    const int nsteps = timing ? 0 : std::atoi(argv[nu_mode ? 4 : 3]);
     {
         std::ifstream cf(in + "/cfg.txt");
         std::string k;
@@ -423,6 +502,26 @@ int run(int argc, char **argv)
         memcpy_dd(d_owner_prev, d_owner, L * 4);
     }
     CU(cuCtxSynchronize());
+    if (nu_mode) {
+        f.clear(); f.shrink_to_fit(); g.clear(); g.shrink_to_fit();
+        const int every = std::atoi(argv[5]);
+        if (every <= 0) { std::fprintf(stderr, "every must be positive\n"); return 2; }
+        std::vector<double> rows;
+        double row[7];
+        for (int s = 1; s <= nsteps; ++s) {
+            step();
+            if (s % every == 0) {
+                CU(cuCtxSynchronize());
+                nu_row(s, row);
+                rows.insert(rows.end(), row, row + 7);
+            }
+        }
+        dump(argv[6], rows.data(), rows.size() * 8);
+        CU(cuModuleUnload(mod));
+        CU(cuDevicePrimaryCtxRelease(dev));
+        std::printf("ref_driver: %d steps, %zu Nu rows\n", nsteps, rows.size() / 7);
+        return 0;
+    }
     if (timing) {
         f.clear(); f.shrink_to_fit(); g.clear(); g.shrink_to_fit();
         const int warm = std::atoi(argv[4]), steps = std::atoi(argv[5]);
@@ -459,13 +558,44 @@ int run(int argc, char **argv)
 
     for (int s = 0; s < nsteps; ++s) step();
 
-    std::vector<char> buf(P);
-    CU(cuMemcpyDtoH(buf.data(), d_f, P)); dump(out + "/f.bin", buf.data(), P);
-    CU(cuMemcpyDtoH(buf.data(), d_g, P)); dump(out + "/g.bin", buf.data(), P);
-    std::vector<double> mac(6 * (size_t)L);
+    const long long stride = cfg.count("sample_stride") ? (long long)cfg["sample_stride"] : 1;
     CUdeviceptr mp[6] = {d_rho, d_ux, d_uy, d_uz, d_phi, d_fx};
-    for (int k = 0; k < 6; ++k) CU(cuMemcpyDtoH(mac.data() + k * L, mp[k], S));
-    dump(out + "/macros.bin", mac.data(), mac.size() * 8);
+    if (stride > 1) {
+        f.clear(); f.shrink_to_fit(); g.clear(); g.shrink_to_fit();
+        auto fs = sampled(d_f, 27, stride), gs = sampled(d_g, 27, stride);
+        dump(out + "/f.bin", fs.data(), fs.size() * 8);
+        dump(out + "/g.bin", gs.data(), gs.size() * 8);
+        std::vector<double> mac;
+        for (int k = 0; k < 6; ++k) {
+            auto m = sampled(mp[k], 1, stride);
+            mac.insert(mac.end(), m.begin(), m.end());
+        }
+        dump(out + "/macros.bin", mac.data(), mac.size() * 8);
+        std::vector<double> plane(L), norms;
+        for (CUdeviceptr d : {d_f, d_g}) {
+            for (int i = 0; i < 27; ++i) {
+                CU(cuMemcpyDtoH(plane.data(), d + (size_t)i * L * 8, L * 8));
+                double s1 = 0.0, s2 = 0.0;
+                for (long long n = 0; n < L; ++n) { s1 += plane[n]; s2 += plane[n] * plane[n]; }
+                norms.push_back(s1);
+                norms.push_back(s2);
+            }
+        }
+        // [f or g][direction][sum, sum of squares] reordered to [direction][f sum, f sq, g sum, g sq]
+        std::vector<double> fgn(27 * 4);
+        for (int i = 0; i < 27; ++i) {
+            fgn[4 * i + 0] = norms[2 * i]; fgn[4 * i + 1] = norms[2 * i + 1];
+            fgn[4 * i + 2] = norms[54 + 2 * i]; fgn[4 * i + 3] = norms[54 + 2 * i + 1];
+        }
+        dump(out + "/fgnorm.bin", fgn.data(), fgn.size() * 8);
+    } else {
+        std::vector<char> buf(P);
+        CU(cuMemcpyDtoH(buf.data(), d_f, P)); dump(out + "/f.bin", buf.data(), P);
+        CU(cuMemcpyDtoH(buf.data(), d_g, P)); dump(out + "/g.bin", buf.data(), P);
+        std::vector<double> mac(6 * (size_t)L);
+        for (int k = 0; k < 6; ++k) CU(cuMemcpyDtoH(mac.data() + k * L, mp[k], S));
+        dump(out + "/macros.bin", mac.data(), mac.size() * 8);
+    }
     if (NP > 0) {
         std::vector<double> rows((size_t)NP * 33), col(NP);
         CUdeviceptr *src[10] = {d_pos, d_vel, d_facc, d_fprev, d_fprev2, d_th, d_omg, d_tacc, d_tprev, d_tprev2};

@@ -39,3 +39,13 @@ def rel_l2(a, b):
     b = np.asarray(b, dtype=np.float64)
     den = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (den if den > 0 else 1.0))
+
+
+@pytest.fixture(scope="session")
+def ref_driver(lib_built, oracle_mod):
+    """The reference-pin driver (oracle/ref_pin/ref_driver.cpp), built once per session; skips
+    where the reference's cubins were not built (they exist only where its sources are)."""
+    import refpin
+    if not refpin.have_cubins():
+        pytest.skip("reference pin cubins are built only where the reference sources exist")
+    return refpin.build_driver()

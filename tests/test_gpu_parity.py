@@ -299,9 +299,15 @@ def test_links_contacts_new_fluid_bit_exact_at_identical_state(env):
     cs, co = s.contacts(), o.contacts()
     assert len(cs[0]) >= 2
     assert np.array_equal(cs[0], co[0]) and np.array_equal(cs[1], co[1])
-    # contact forces are summed in the same (ascending partner) order: bit-exact history columns
+    # Force (columns 6-8) = IBB momentum exchange + the contact and wall forces of the step's start
+    # positions (pforces.cu:6-76); torque (21-23).  The contact sums run in the same ascending-
+    # partner order on both sides; the IBB sums in a fixed tree order here and link order in the
+    # oracle, so the columns agree to rounding.
     ps, po = s.particles(), o.particles()
-    # force_prev holds last step's total; this step's contact part is inside force (col 6-8)
+    for cols in (slice(6, 9), slice(9, 12), slice(12, 15), slice(21, 24)):
+        scale = max(np.abs(po[:, cols]).max(), 1e-300)
+        assert np.abs(ps[:, cols] - po[:, cols]).max() <= 1e-12 * scale, cols
+    assert np.abs(po[:2, 6:9]).max() > 0.1                # the first pair is in contact
     assert np.array_equal(s.flags(), o.flags())
     nfs, nfo = s.new_fluid(), o.new_fluid()
     assert np.array_equal(nfs[0], nfo[0]) and np.array_equal(nfs[1], nfo[1])
