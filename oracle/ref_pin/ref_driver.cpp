@@ -575,10 +575,17 @@ int run(int argc, char **argv)
         for (CUdeviceptr d : {d_f, d_g}) {
             for (int i = 0; i < 27; ++i) {
                 CU(cuMemcpyDtoH(plane.data(), d + (size_t)i * L * 8, L * 8));
-                double s1 = 0.0, s2 = 0.0;
-                for (long long n = 0; n < L; ++n) { s1 += plane[n]; s2 += plane[n] * plane[n]; }
-                norms.push_back(s1);
-                norms.push_back(s2);
+                // compensated (Neumaier) sums: accurate to a few units in the last place, so the
+                // comparison measures the fields and not this summation order
+                double s1 = 0.0, c1 = 0.0, s2 = 0.0, c2 = 0.0;
+                auto add = [](double &sum, double &comp, double v) {
+                    const double t = sum + v;
+                    comp += std::fabs(sum) >= std::fabs(v) ? (sum - t) + v : (v - t) + sum;
+                    sum = t;
+                };
+                for (long long n = 0; n < L; ++n) { add(s1, c1, plane[n]); add(s2, c2, plane[n] * plane[n]); }
+                norms.push_back(s1 + c1);
+                norms.push_back(s2 + c2);
             }
         }
         // [f or g][direction][sum, sum of squares] reordered to [direction][f sum, f sq, g sum, g sq]

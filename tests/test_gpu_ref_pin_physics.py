@@ -8,6 +8,8 @@ right measure or the configuration is the full-size one.
   leaves the physical regime at that density ratio (tests/test_oracle_unstable_cases.py records
   where): particle columns, solid owners, link sets and new-fluid lists, and sampled fields.
 """
+import math
+
 import numpy as np
 import pytest
 
@@ -50,30 +52,67 @@ def test_long_run_nusselt_steady_convection_against_reference(ref_driver, tmp_pa
 
 STRIDE = 9973          # sampled nodes of the full-size comparison (a prime: every residue class)
 PIN_STEPS = 5
+FIELD_STEPS = 2
+
+
+def _field_checks(s, out, L, tol):
+    """Sampled populations and macroscopic fields, and per-direction sums and sums of squares of
+    f and g (exact sums here, compensated sums in the driver); returns the largest relative
+    difference seen."""
+    fs, gs = s.fg()
+    fs, gs = fs.reshape(27, L), gs.reshape(27, L)
+    fn = np.fromfile(out / "fgnorm.bin").reshape(27, 4)
+    ours = np.array([[math.fsum(fs[i]), math.fsum(fs[i] * fs[i]), math.fsum(gs[i]), math.fsum(gs[i] * gs[i])]
+                     for i in range(27)])
+    worst = 0.0
+    for c in (1, 3):                  # sums of squares, per direction
+        worst = max(worst, float(np.max(np.abs(ours[:, c] / fn[:, c] - 1.0))))
+    for c, sq in ((0, 1), (2, 3)):    # plain sums against the scale of the population
+        worst = max(worst, float(np.max(np.abs(ours[:, c] - fn[:, c]) / np.sqrt(fn[:, sq] * L))))
+    fr = np.fromfile(out / "f.bin").reshape(27, -1)
+    gr = np.fromfile(out / "g.bin").reshape(27, -1)
+    fsm, gsm = fs[:, ::STRIDE], gs[:, ::STRIDE]
+    assert fsm.shape == fr.shape
+    worst = max(worst, np.linalg.norm(gsm - gr) / np.linalg.norm(gr), np.linalg.norm(fsm - fr) / np.linalg.norm(gr))
+    mr = np.fromfile(out / "macros.bin").reshape(6, -1)
+    m = s.macros()
+    for k, name in enumerate(["rho", "ux", "uy", "uz", "phi", "force_x"]):
+        den = max(np.linalg.norm(mr[k]), 1e-3 * np.linalg.norm(mr[4]))
+        worst = max(worst, np.linalg.norm(m[name][::STRIDE] - mr[k]) / den)
+    assert worst < tol, worst
+    return worst
 
 
 def test_config3_density_ratio_1p5_first_steps_against_reference(ref_driver, tmp_path):
     """The particle-laden configuration at density ratio 1.5: 320x320x160, Ra = 1e8, 1000 spheres
     of diameter 16 placed by the reference's glibc rejection sampler, seeded +-1e-3 start.  The
-    spheres accelerate at (1 - 1/1.5) g0 = 0.33 lattice units per step^2 (move.cu:47,63); the
-    first five steps (every sphere inside the box and the lattice finite, checked on librbtp
-    first so that the reference's kernels never see an escaped sphere) agree with the reference's
-    kernels: particle columns within 1e-8 of each column's scale (the heat column, a sum of some
-    7,000 link terms per sphere that the reference adds with atomics in arbitrary order, differs by
-    1.3e-9 of its scale at this violent state; every other column by less than 1e-10), owners, link
-    sets and new-fluid lists bit-exact, sampled populations and macroscopic fields within 1e-12
-    relative L2, and the per-direction sums of squares of f and g within 1e-12."""
+    spheres accelerate at (1 - 1/1.5) g0 = 0.33 lattice units per step^2 (move.cu:47,63).  Checked
+    on librbtp first, so that the reference's kernels never see an escaped sphere: after five steps
+    every sphere is inside the box and the lattice is finite.  Against the reference's kernels:
+    after two steps (while the flow is still near rest) the sampled populations and macroscopic
+    fields and the per-direction sums of squares of f and g agree within 1e-12; after five steps
+    the particle columns agree within 1e-8 of each column's scale and the owners, link sets and
+    new-fluid lists bit for bit.  By step five the density deviation near the spheres reaches
+    about -2 (the method has left its range of validity), rounding differences grow by orders of
+    magnitude per step there, and the fields agree to 5e-9 (asserted below 1e-7); the heat
+    column, a sum of some 7,000 link terms per sphere that the reference adds with atomics in
+    arbitrary order, agrees to 1.3e-9 of its scale."""
     case = "ref_particle_laden"
     cfg = refpin.cfg_of(case, rho_particle_ratio=1.5)
     der = derive(cfg)
     assert der.npart == 1000 and der.particle_radius == 8.0
+    L = cfg.nodes
     s = Solver(cfg)
     s.initialize()                                  # placement of pinit.cu:97-144
     p0 = s.particles()
     f, g, f7 = W.initial_state(cfg, seed=1)
     s.load_state(f, g, f7, p0)
     del f, g, f7
-    s.step(PIN_STEPS, macros_last=True)
+    s.step(FIELD_STEPS, macros_last=True)
+    out2 = refpin.run(ref_driver, case, tmp_path / "s2", cfg, None, None, None, p0, FIELD_STEPS, timeout=1800,
+                      synthetic=1, seed=1, amp=1e-3, sample_stride=STRIDE)
+    print(f"ratio 1.5, {FIELD_STEPS} steps: fields within {_field_checks(s, out2, L, 1e-12):.2e}")
+    s.step(PIN_STEPS - FIELD_STEPS, macros_last=True)
     ps = s.particles()
     r = der.particle_radius
     inside = ((ps[:, 0] > r) & (ps[:, 0] < cfg.lx - r) & (ps[:, 1] > r) & (ps[:, 1] < cfg.ly - r)
@@ -82,7 +121,7 @@ def test_config3_density_ratio_1p5_first_steps_against_reference(ref_driver, tmp
     vmax = np.sqrt((ps[:, 3:6] ** 2).sum(1)).max()
     print(f"ratio 1.5, {PIN_STEPS} steps: max sphere speed {vmax:.3f} lattice units per step")
 
-    out = refpin.run(ref_driver, case, tmp_path, cfg, None, None, None, p0, PIN_STEPS, timeout=1800,
+    out = refpin.run(ref_driver, case, tmp_path / "s5", cfg, None, None, None, p0, PIN_STEPS, timeout=1800,
                      synthetic=1, seed=1, amp=1e-3, sample_stride=STRIDE)
     pr = np.fromfile(out / "particles.bin").reshape(-1, 33)
     scale = np.maximum(np.abs(pr).max(0), 1e-300)
@@ -96,25 +135,5 @@ def test_config3_density_ratio_1p5_first_steps_against_reference(ref_driver, tmp
     node, pid = s.new_fluid()
     order = np.argsort(nf[:, 0], kind="stable")
     assert len(node) > 1000 and np.array_equal(node, nf[order, 0]) and np.array_equal(pid, nf[order, 1])
-
-    L = cfg.nodes
-    fs, gs = s.fg()
-    fs, gs = fs.reshape(27, L), gs.reshape(27, L)
-    fn = np.fromfile(out / "fgnorm.bin").reshape(27, 4)
-    ours = np.stack([fs.sum(1), (fs * fs).sum(1), gs.sum(1), (gs * gs).sum(1)], axis=1)
-    for c in (1, 3):                  # sums of squares, per direction
-        np.testing.assert_allclose(ours[:, c], fn[:, c], rtol=1e-12, atol=0)
-    for c, sq in ((0, 1), (2, 3)):    # plain sums against the scale of the population
-        assert np.all(np.abs(ours[:, c] - fn[:, c]) <= 1e-12 * np.sqrt(fn[:, sq] * L))
-    fr = np.fromfile(out / "f.bin").reshape(27, -1)
-    gr = np.fromfile(out / "g.bin").reshape(27, -1)
-    fsm, gsm = fs[:, ::STRIDE], gs[:, ::STRIDE]
-    assert fsm.shape == fr.shape
-    assert np.linalg.norm(gsm - gr) / np.linalg.norm(gr) < 1e-12
-    assert np.linalg.norm(fsm - fr) / np.linalg.norm(gr) < 1e-12
-    mr = np.fromfile(out / "macros.bin").reshape(6, -1)
-    m = s.macros()
-    for k, name in enumerate(["rho", "ux", "uy", "uz", "phi", "force_x"]):
-        den = max(np.linalg.norm(mr[k]), 1e-3 * np.linalg.norm(mr[4]))
-        assert np.linalg.norm(m[name][::STRIDE] - mr[k]) / den < 1e-12, name
+    print(f"ratio 1.5, {PIN_STEPS} steps: fields within {_field_checks(s, out, L, 1e-7):.2e}")
     s.close()
