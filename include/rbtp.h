@@ -133,7 +133,13 @@ int  rbtp_init_fresh(rbtp_handle *h);
  *                force is rebuilt from its phi as forcing() does (initial.cu:230);  NULL means
  *                phi = sum_i g_i;
  *   particles  : npart*RBTP_PARTICLE_COLS (pos file columns) or NULL when npart == 0.
- * Then build_links() and flags_prev = flags (initial.cu:231-235). */
+ * Then build_links() and flags_prev = flags (initial.cu:231-235).
+ * The arrays are read once, by one import kernel that writes the storage format, the flow fields
+ * and the buoyancy force in the same pass.  Page-locked host memory (cudaHostAlloc'd or
+ * registered) and device memory are read in place, the former over the host link; ordinary
+ * pageable host memory is copied in chunks of 2^20 nodes through two temporary device staging
+ * slots (about 1 GB, freed before the call returns), each chunk's import overlapping the next
+ * chunk's copy.  The call returns once the import has completed. */
 int  rbtp_load_state(rbtp_handle *h, const double *f, const double *g, const double *flow7,
                      const double *particles);
 /* Restart from the reference's files in dir: fg%09d.dat, %09d.dat, pos/pos_%09d.txt. */
@@ -145,8 +151,12 @@ int  rbtp_load_restart(rbtp_handle *h, const char *dir, int step);
  * one pull-stream/collide kernel per step plus the particle kernels.  Macroscopic fields are
  * materialised on steps that hit the config's
  * output cadence (NDIAG, NNUOUT, NFLOWOUT, NEND) and, with RBTP_STEP_MACROS_LAST, on the last
- * step of the call. */
+ * step of the call.  The dissipation fields ted/Ked of output_flow (compute_Ked/compute_ted,
+ * collision.cu:91-198) are produced on flow-output steps (NFLOWOUT, NEND) and, with
+ * RBTP_STEP_FLOW_LAST, on the last step of the call; they need an FP64 copy of the step's
+ * post-collision populations (2 x 27 L doubles, allocated on first use and kept). */
 #define RBTP_STEP_MACROS_LAST 1u
+#define RBTP_STEP_FLOW_LAST   2u
 int  rbtp_step(rbtp_handle *h, int nsteps);
 int  rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags);
 int  rbtp_current_step(const rbtp_handle *h, int *istep);
@@ -284,6 +294,13 @@ int  rbtp_server_stats(rbtp_server *s, double *node_updates, double *steps, doub
  * series, and the server clock continues.  No counterpart in the reference. */
 int  rbtp_server_checkpoint(rbtp_server *s, const char *dir);
 int  rbtp_server_restore(rbtp_server *s, const char *dir);
+
+/* ---- calibration -------------------------------------------------------------------------------- */
+/* The FP64 fused multiply-add rate of the current device in flop/s (2 per FMA), measured by a
+ * microkernel with independent chains on every SM and timed with CUDA events (best of four runs
+ * after a warm-up): the compute roofline of the FP64 storage mode, whose step is bound by the FP64
+ * pipe rather than by HBM.  No counterpart in the reference. */
+int  rbtp_fp64_fma_rate(double *flops_per_s);
 
 /* ---- allocation-free diagnostic sums ----------------------------------------------------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device memory — code hosted in

@@ -108,7 +108,7 @@ cudaError_t aux_from_host(rbtp_handle *h, const double *src)
 }
 
 // Build the current solid flags and the IBB link slabs from the current particle positions
-// (build_links, links.cu:572-685).
+// (build_links, links.cu:143-256).
 int build_links(rbtp_handle *h, int *owner, bool pgeo_fresh = false)
 {
     CK(launch_mark(h->geo, h->ph, h->pb, owner, h->stream, !pgeo_fresh));
@@ -146,6 +146,103 @@ int plane_sums(rbtp_handle *h)
                        cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     h->plane_valid = true;
+    return RBTP_OK;
+}
+
+// The device address under which the kernels can read `bytes` of a caller's buffer directly:
+// the buffer itself for device or managed memory of this device, the device alias of page-locked
+// (cudaHostAlloc'd or registered) host memory when the whole range lies in one such allocation;
+// nullptr when the buffer has to be copied (ordinary pageable host memory).
+const void *device_view(const rbtp_handle *h, const void *p, size_t bytes)
+{
+    cudaPointerAttributes a{}, b{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if ((a.type == cudaMemoryTypeDevice && a.device == h->device) || a.type == cudaMemoryTypeManaged) return p;
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    const char *last = static_cast<const char *>(p) + bytes - 1;
+    if (cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (b.type != cudaMemoryTypeHost ||
+        static_cast<const char *>(b.devicePointer) - static_cast<const char *>(a.devicePointer) != (ptrdiff_t)(bytes - 1))
+        return nullptr;
+    return a.devicePointer;
+}
+
+// Restart import (initial.cu:194-236, array form) of f, g (27 L doubles each) and the optional
+// seven flow fields (7 L doubles): one pass of k_import_nodes writes the storage slots, the flow
+// fields (or the moments of f and g) and the buoyancy auxiliary.  Sources the device can read are
+// read in place; pageable host buffers are copied in chunks of nodes (one strided 2D copy per
+// array and chunk) into two staging slots, alternating so that the import of one chunk overlaps
+// the copy of the next.  No full-size FP64 scratch is allocated.
+int import_state(rbtp_handle *h, const double *f, const double *g, const double *flow7)
+{
+    const long long L = h->geo.L;
+    const size_t P = 27 * (size_t)L * sizeof(double), F7 = 7 * (size_t)L * sizeof(double);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    void *fs = h->f[0], *gs = h->g[0];
+    const double *df = static_cast<const double *>(device_view(h, f, P));
+    const double *dg = static_cast<const double *>(device_view(h, g, P));
+    const double *d7 = flow7 ? static_cast<const double *>(device_view(h, flow7, F7)) : nullptr;
+    if (df && dg && (!flow7 || d7)) {
+        CK(launch_import_nodes(h->mode, h->geo, h->ph, 0, L, df, dg, L, d7, L, fs, gs, h->faux,
+                               h->rho, h->ux, h->uy, h->uz, h->phi, h->ted, h->ked, sms, h->stream));
+        return RBTP_OK;
+    }
+    // staged: chunks of C nodes, slot = f[27][C], g[27][C], flow7[7][C]
+    const long long C = std::min<long long>(L, 1LL << 20);
+    const size_t slot = (size_t)(27 + 27 + 7) * (size_t)C;
+    int maxpitch = 0;
+    cudaDeviceGetAttribute(&maxpitch, cudaDevAttrMaxPitch, h->device);
+    double *stage = nullptr;
+    CK(dalloc(&stage, 2 * slot));
+    cudaStream_t cs = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};   // copied[2], imported[2]
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+    // the copy stream starts after the work already queued on the handle's stream
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2], h->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[3], h->stream);
+    for (long long n0 = 0, c = 0; n0 < L && e == cudaSuccess; n0 += C, ++c) {
+        const int b = (int)(c & 1);
+        const long long cnt = std::min<long long>(C, L - n0);
+        double *sf = stage + b * slot, *sg = sf + 27 * C, *s7 = sg + 27 * C;
+        const size_t w = (size_t)cnt * sizeof(double), spitch = (size_t)L * sizeof(double),
+                     dpitch = (size_t)C * sizeof(double);
+        // rows of one array: a 2D copy, or one copy per row where the source pitch exceeds the
+        // largest pitch a 2D copy takes
+        auto rows = [&](double *dst, const double *src, int nrow) {
+            if (spitch <= (size_t)maxpitch)
+                return cudaMemcpy2DAsync(dst, dpitch, src, spitch, w, nrow, cudaMemcpyDefault, cs);
+            cudaError_t r = cudaSuccess;
+            for (int k = 0; k < nrow && r == cudaSuccess; ++k)
+                r = cudaMemcpyAsync(dst + (size_t)k * C, src + (size_t)k * L, w, cudaMemcpyDefault, cs);
+            return r;
+        };
+        e = cudaStreamWaitEvent(cs, ev[2 + b], 0);          // slot b no longer read by its last import
+        if (e == cudaSuccess) e = rows(sf, f + n0, 27);
+        if (e == cudaSuccess) e = rows(sg, g + n0, 27);
+        if (e == cudaSuccess && flow7) e = rows(s7, flow7 + n0, 7);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[b], cs);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, ev[b], 0);
+        if (e == cudaSuccess)
+            e = launch_import_nodes(h->mode, h->geo, h->ph, n0, cnt, sf, sg, C, flow7 ? s7 : nullptr, C, fs, gs,
+                                    h->faux, h->rho, h->ux, h->uy, h->uz, h->phi, h->ted, h->ked, sms, h->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[2 + b], h->stream);
+    }
+    // the staging slots are released only once every import has run
+    const cudaError_t es = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) e = es;
+    for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    if (cs) cudaStreamDestroy(cs);
+    cudaFree(stage);
+    CK(e);
     return RBTP_OK;
 }
 
@@ -508,12 +605,8 @@ int rbtp_load_state(rbtp_handle *h, const double *f, const double *g, const doub
     if (!h || !f || !g) return RBTP_ERR_ARG;
     const int np = h->pb.np;
     if (np > 0 && !particles) return fail(h, RBTP_ERR_ARG, "particle state required");
-    int s = ensure_scratch(h);
+    int s = import_state(h, f, g, flow7);
     if (s) return s;
-    const size_t L = (size_t)h->geo.L, P = 27 * L;
-    CK(cudaMemcpyAsync(h->fcol, f, P * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->gcol, g, P * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    CK(launch_home_import(h->mode, h->geo, h->ph, h->fcol, h->gcol, h->f[0], h->g[0], h->stream));
     h->cur = 0;
     h->phase = PHASE_HOME;
     h->ocur = 0;
@@ -525,16 +618,6 @@ int rbtp_load_state(rbtp_handle *h, const double *f, const double *g, const doub
         s = build_links(h, h->owner[0]);
         if (s) return s;
     }
-    if (flow7) {
-        double *dst[7] = {h->rho, h->ux, h->uy, h->uz, h->phi, h->ted, h->ked};
-        for (int k = 0; k < 7; ++k)
-            CK(cudaMemcpyAsync(dst[k], flow7 + k * L, L * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    } else {
-        CK(launch_macros_from_home(h->geo, h->fcol, h->gcol, h->rho, h->ux, h->uy, h->uz, h->phi, h->stream));
-        CK(cudaMemsetAsync(h->ted, 0, L * sizeof(double), h->stream));
-        CK(cudaMemsetAsync(h->ked, 0, L * sizeof(double), h->stream));
-    }
-    CK(launch_forcing(h->mode, h->geo, h->ph, h->phi, h->faux, h->stream));
     h->istep = h->cfg.continuous_steps > 0 ? h->cfg.continuous_steps : 0;
     h->initialised = true;
     h->macros_valid = true;
@@ -553,9 +636,10 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
     const rbtp_config &c = h->cfg;
     for (int k = 1; k <= nsteps; ++k) {
         const int istep = h->istep + 1;
-        const bool last = (flags & RBTP_STEP_MACROS_LAST) && k == nsteps;
-        const bool flow = cadence(istep, c.nflowout) || istep == c.nend || last;
-        const bool macro = flow || cadence(istep, c.ndiag) || cadence(istep, c.nnuout);
+        const bool last = k == nsteps;
+        const bool flow = cadence(istep, c.nflowout) || istep == c.nend || (last && (flags & RBTP_STEP_FLOW_LAST));
+        const bool macro = flow || cadence(istep, c.ndiag) || cadence(istep, c.nnuout) ||
+                           (last && (flags & RBTP_STEP_MACROS_LAST));
         int out = OUT_NONE;
         if (flow) out = OUT_MACROS_COL;
         else if (macro) out = OUT_MACROS;

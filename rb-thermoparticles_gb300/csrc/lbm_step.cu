@@ -16,19 +16,11 @@
 // values split into a pair-symmetric and a pair-antisymmetric part.  The g source term of
 // collision.cu:57-88 reduces to w_i c_i.V with one per-node vector V because it is linear in c_i;
 // its first pass (the non-equilibrium first moment) is sum_i c_i g_i - phi u exactly.
+#include <algorithm>
+
 #include "step_node.cuh"
 
 namespace rbtp {
-
-namespace {
-
-struct NodeIdx {
-    int ix, iy, iz;
-    long long node;
-};
-
-
-}  // namespace
 
 namespace {
 
@@ -125,6 +117,73 @@ __global__ void k_home_import(const Geo geo, const Phys ph, const double *fin, c
         ST::st_f(fout + (long long)i * geo.L + n, (R)fin[(long long)i * geo.L + n], w, ph.t0);
         ST::st_g(gout + (long long)i * geo.L + n, (R)gin[(long long)i * geo.L + n], w, sh);
     });
+}
+
+// Restart import of the nodes n0 .. n0 + count - 1 in one pass (the array form of
+// load_restart_state, initial.cu:194-236): the FP64 home-layout populations f_i, g_i (node n0 + k
+// of direction i at f[i * pstride + k]) into the storage slots (i, n); the seven flow fields rho,
+// ux, uy, uz, phi, ted, ked (field j at f7[j * fstride + k]) into the device fields, or, with f7
+// null, macrovar's moments of the imported populations with zero force (macrovar.cu:3-34) and
+// ted = ked = 0; and forcing()'s buoyancy F_x = g0 beta (phi - T0) (macrovar.cu:45) from phi.
+// The sources are device memory or page-locked host memory read directly through its device
+// alias; every source element is read once, in coalesced rows of one direction.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_import_nodes(const Geo geo, const Phys ph, long long n0, long long count,
+                                                      const double *__restrict__ f, const double *__restrict__ g,
+                                                      long long pstride, const double *__restrict__ f7,
+                                                      long long fstride, void *fout_, void *gout_, void *faux_,
+                                                      double *rho, double *ux, double *uy, double *uz,
+                                                      double *phi, double *ted, double *ked)
+{
+    using ST = Store<MODE>;
+    using S = typename ST::S;
+    using R = typename ST::R;
+    S *fout = static_cast<S *>(fout_);
+    S *gout = static_cast<S *>(gout_);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+        const long long n = n0 + k;
+        const double sh = gshift(ph, (int)(n % geo.lx));
+        double r = 0, jx = 0, jy = 0, jz = 0, p = 0;
+        unroll<27>([&](auto I) {
+            constexpr int i = decltype(I)::value;
+            constexpr double w = dweight(i);
+            const double fv = f[(long long)i * pstride + k];
+            const double gv = g[(long long)i * pstride + k];
+            const long long slot = (long long)i * geo.L + n;
+            if constexpr (ST::PAIRED) {
+                S v;   // both halves of the (f_i, g_i) slot, stored at once
+                ST::st_f(&v, (R)fv, w, ph.t0);
+                ST::st_g(&v, (R)gv, w, sh);
+                fout[slot] = v;
+            } else {
+                ST::st_f(fout + slot, (R)fv, w, ph.t0);
+                ST::st_g(gout + slot, (R)gv, w, sh);
+            }
+            r += fv;
+            jx += dcx(i) * fv;
+            jy += dcy(i) * fv;
+            jz += dcz(i) * fv;
+            p += gv;
+        });
+        double phv;
+        if (f7) {
+            rho[n] = f7[k];
+            ux[n] = f7[fstride + k];
+            uy[n] = f7[2 * fstride + k];
+            uz[n] = f7[3 * fstride + k];
+            phv = f7[4 * fstride + k];
+            ted[n] = f7[5 * fstride + k];
+            ked[n] = f7[6 * fstride + k];
+        } else {
+            rho[n] = r; ux[n] = jx; uy[n] = jy; uz[n] = jz;
+            phv = p;
+            ted[n] = 0.0;
+            ked[n] = 0.0;
+        }
+        phi[n] = phv;
+        static_cast<typename ST::A *>(faux_)[n] = (typename ST::A)(ph.grav0 * ph.beta * (phv - ph.t0));
+    }
 }
 
 // init_f / init_g (initial.cu:335-397): deviation-form rest f = 0; g from the equilibrium at
@@ -258,6 +317,22 @@ cudaError_t launch_home_import(int mode, const Geo &geo, const Phys &ph, const d
                                const double *gin, void *fout, void *gout, cudaStream_t st)
 {
     RBTP_MODE_DISPATCH(mode, (k_home_import<M><<<lin_blocks(geo.L, 256), 256, 0, st>>>(geo, ph, fin, gin, fout, gout)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_import_nodes(int mode, const Geo &geo, const Phys &ph, long long n0, long long count,
+                                const double *f, const double *g, long long pstride, const double *f7,
+                                long long fstride, void *fout, void *gout, void *faux, double *rho,
+                                double *ux, double *uy, double *uz, double *phi, double *ted, double *ked,
+                                int sms, cudaStream_t st)
+{
+    if (count <= 0) return cudaSuccess;
+    // a grid of a few blocks per SM keeps many independent row loads in flight (host-memory
+    // sources answer with a long latency) without one block per node
+    const long long want = (count + 255) / 256;
+    const unsigned blocks = (unsigned)std::min<long long>(want, 8LL * std::max(sms, 1));
+    RBTP_MODE_DISPATCH(mode, (k_import_nodes<M><<<blocks, 256, 0, st>>>(geo, ph, n0, count, f, g, pstride, f7, fstride,
+                                                                      fout, gout, faux, rho, ux, uy, uz, phi, ted, ked)));
     return cudaGetLastError();
 }
 

@@ -295,6 +295,13 @@ cudaError_t launch_home_export(int mode, const Geo &geo, const Phys &ph, const v
                                const void *gin, double *fout, double *gout, cudaStream_t st);
 cudaError_t launch_home_import(int mode, const Geo &geo, const Phys &ph, const double *fin,
                                const double *gin, void *fout, void *gout, cudaStream_t st);
+// One-pass restart import of nodes n0 .. n0 + count - 1 (populations, flow fields or moments,
+// buoyancy auxiliary); sources in device memory or device-visible page-locked host memory.
+cudaError_t launch_import_nodes(int mode, const Geo &geo, const Phys &ph, long long n0, long long count,
+                                const double *f, const double *g, long long pstride, const double *f7,
+                                long long fstride, void *fout, void *gout, void *faux, double *rho,
+                                double *ux, double *uy, double *uz, double *phi, double *ted, double *ked,
+                                int sms, cudaStream_t st);
 cudaError_t launch_fresh_init(int mode, const Geo &geo, const Phys &ph, void *f, void *g,
                               void *faux, double *rho, double *ux, double *uy, double *uz,
                               double *phi, cudaStream_t st);

@@ -29,6 +29,7 @@ STATUS = {
 }
 STORE_F64, STORE_F32, STORE_F16S = 0, 1, 2
 STEP_MACROS_LAST = 1
+STEP_FLOW_LAST = 2
 PARTICLE_COLS = 33
 
 # Column names of the particle-state rows (pos/pos_%09d.txt after the pid).
@@ -187,6 +188,7 @@ SIGNATURES = [
     ("rbtp_server_stats", C.c_int, [_H, _DP, _DP, _DP, _DP]),
     ("rbtp_server_checkpoint", C.c_int, [_H, C.c_char_p]),
     ("rbtp_server_restore", C.c_int, [_H, C.c_char_p]),
+    ("rbtp_fp64_fma_rate", C.c_int, [C.POINTER(C.c_double)]),
     ("rbtp_plane_sums_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                           C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                           C.c_double, C.c_void_p, C.c_void_p]),
@@ -290,12 +292,24 @@ class Solver:
             particles = np.ascontiguousarray(particles, dtype=np.float64)
         _check(self.lib.rbtp_load_state(self._h, _dp(f), _dp(g), _dp(flow7), _dp(particles)), self._h)
 
+    def load_state_ptr(self, f_addr: int, g_addr: int, flow7_addr: Optional[int] = None,
+                       particles: Optional[np.ndarray] = None) -> None:
+        """rbtp_load_state from raw addresses (device memory, page-locked or pageable host memory of
+        27 L, 27 L and 7 L doubles), e.g. the data_ptr() of tensors."""
+        if particles is not None:
+            particles = np.ascontiguousarray(particles, dtype=np.float64)
+        cast = lambda a: None if a is None else C.cast(C.c_void_p(a), _DP)  # noqa: E731
+        _check(self.lib.rbtp_load_state(self._h, cast(f_addr), cast(g_addr), cast(flow7_addr), _dp(particles)),
+               self._h)
+
     def load_restart(self, directory: str, step: int) -> None:
         _check(self.lib.rbtp_load_restart(self._h, directory.encode(), step), self._h)
 
     # -- the time loop (main.cu:32-85) --------------------------------------------------------
-    def step(self, nsteps: int = 1, macros_last: bool = False) -> None:
-        flags = STEP_MACROS_LAST if macros_last else 0
+    def step(self, nsteps: int = 1, macros_last: bool = False, flow_last: bool = False) -> None:
+        """Advance nsteps; macros_last materialises the macroscopic fields on the last step,
+        flow_last also the dissipation fields of a flow-output step."""
+        flags = (STEP_MACROS_LAST if macros_last else 0) | (STEP_FLOW_LAST if flow_last else 0)
         _check(self.lib.rbtp_step_ex(self._h, nsteps, flags), self._h)
 
     @property
@@ -488,6 +502,13 @@ class Batch:
             pass
 
 
+def fp64_fma_rate() -> float:
+    """Measured FP64 FMA rate of the current device in flop/s (rbtp_fp64_fma_rate)."""
+    v = C.c_double()
+    _check(load_library().rbtp_fp64_fma_rate(C.byref(v)))
+    return v.value
+
+
 def footprint(cfg: Config) -> int:
     b = C.c_size_t()
     _check(load_library().rbtp_footprint(C.byref(cfg), C.byref(b)))
@@ -558,4 +579,4 @@ def _b(s: Optional[str]):
 
 __all__ = ["Config", "Derived", "NuRow", "Solver", "Batch", "BatchStats", "Server", "footprint", "RbtpError", "load_library", "derive",
            "STORE_F64", "STORE_F32", "STORE_F16S", "PARTICLE_COLS", "PARTICLE_COLUMNS",
-           "SIGNATURES", "LIB_PATH"]
+           "SIGNATURES", "LIB_PATH", "fp64_fma_rate"]

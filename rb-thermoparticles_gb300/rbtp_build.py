@@ -25,7 +25,7 @@ LIBDIR = os.path.join(HERE, "rbtp", "_lib")
 LIB = os.path.join(LIBDIR, "librbtp.so")
 RB3D = os.path.join(LIBDIR, "rb3d")
 
-SOURCES = ["lbm_step.cu", "batch_step.cu", "particles.cu", "diagnostics.cu", "api.cu", "batch.cu", "server.cu", "noalloc.cu"]
+SOURCES = ["lbm_step.cu", "batch_step.cu", "particles.cu", "diagnostics.cu", "api.cu", "batch.cu", "server.cu", "noalloc.cu", "calib.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",

@@ -52,7 +52,7 @@ def test_single_phase_fp64_100_steps(env):
     s.step(1, macros_last=True)
     o.step(1)
     _compare_fields(s, o, tol=1e-14)
-    s.step(99, macros_last=True)
+    s.step(99, macros_last=True, flow_last=True)
     o.step(99)
     _compare_fields(s, o)
     ns, no = np.array(s.nu(100)), np.array(o.nu(100))
