@@ -72,6 +72,14 @@ def lib() -> C.CDLL:
             "orc_link_q": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.c_double, C.c_double, C.c_double, _DP]),
             "orc_set_positions_and_build": (C.c_int, [H, _DP]),
+            "orc_output_dirname": (C.c_int, [C.c_double, C.c_double, C.c_char_p, C.c_size_t]),
+            "orc_write_statistics": (C.c_int, [C.c_char_p, C.c_int, _DP]),
+            "orc_write_nu": (C.c_int, [C.c_char_p, C.c_double, C.POINTER(NuRow)]),
+            "orc_write_profile": (C.c_int, [C.c_char_p, C.c_double, C.c_int, C.c_int, _DP]),
+            "orc_write_flow": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _DP,
+                                         _IP, _DP, C.c_int]),
+            "orc_write_fg": (C.c_int, [C.c_char_p, C.c_int, C.c_long, _DP, _DP]),
+            "orc_write_particles": (C.c_int, [C.c_char_p, C.c_int, C.c_int, _DP]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(_lib, name)
@@ -220,3 +228,48 @@ class Oracle:
     def set_positions_and_build(self, pos_xyz):
         pos = np.ascontiguousarray(pos_xyz, dtype=np.float64).reshape(-1)
         _ck(self.lib.orc_set_positions_and_build(self._h, _dp(pos)), "set_positions")
+
+
+# ---- the reference's output writers (oracle/rbtp_oracle_io.c), fed with the values to write ----
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def output_dirname(rayleigh: float, prandtl: float) -> str:
+    buf = C.create_string_buffer(256)
+    _ck(lib().orc_output_dirname(rayleigh, prandtl, buf, 256), "output_dirname")
+    return buf.value.decode()
+
+
+def write_statistics(directory: str, istep: int, means) -> None:
+    m = _f64(means)
+    _ck(lib().orc_write_statistics(directory.encode(), istep, _dp(m)), "write_statistics")
+
+
+def write_nu(directory: str, rayleigh: float, row) -> None:
+    r = NuRow(*[float(v) for v in row])
+    _ck(lib().orc_write_nu(directory.encode(), rayleigh, C.byref(r)), "write_nu")
+
+
+def write_profile(directory: str, rayleigh: float, istep: int, profile) -> None:
+    p = _f64(profile).reshape(-1)
+    _ck(lib().orc_write_profile(directory.encode(), rayleigh, istep, len(p) // 4, _dp(p)), "write_profile")
+
+
+def write_flow(directory: str, istep: int, cfg: Config, fields7, owner=None, rows=None) -> None:
+    f7 = _f64(fields7).reshape(-1)
+    own = None if owner is None else np.ascontiguousarray(owner, dtype=np.int32)
+    r = None if rows is None else _f64(rows)
+    np_ = 0 if r is None else len(r)
+    _ck(lib().orc_write_flow(directory.encode(), istep, cfg.lx, cfg.ly, cfg.lz, cfg.rho0, _dp(f7), _ip(own),
+                             _dp(r), np_), "write_flow")
+
+
+def write_fg(directory: str, istep: int, f, g) -> None:
+    f, g = _f64(f), _f64(g)
+    _ck(lib().orc_write_fg(directory.encode(), istep, len(f) // 27, _dp(f), _dp(g)), "write_fg")
+
+
+def write_particles(directory: str, istep: int, rows) -> None:
+    r = _f64(rows)
+    _ck(lib().orc_write_particles(directory.encode(), istep, len(r), _dp(r)), "write_particles")

@@ -48,6 +48,16 @@ int  orc_means(orc_sim *s, double means[4]);
 int  orc_profile(orc_sim *s, double *profile);
 int  orc_dissipation(orc_sim *s, double *ted, double *ked);
 
+/* The reference's output writers (rbtp_oracle_io.c), fed with the values to write. */
+int  orc_output_dirname(double rayleigh, double prandtl, char *buf, size_t len);
+int  orc_write_statistics(const char *dir, int istep, const double means[4]);
+int  orc_write_nu(const char *dir, double rayleigh, const rbtp_nu_row *row);
+int  orc_write_profile(const char *dir, double rayleigh, int istep, int lx, const double *profile);
+int  orc_write_flow(const char *dir, int istep, int lx, int ly, int lz, double rho0, const double *fields,
+                    const int *owner, const double *rows, int np);
+int  orc_write_fg(const char *dir, int istep, long L, const double *f, const double *g);
+int  orc_write_particles(const char *dir, int istep, int np, const double *rows);
+
 /* Stand-alone pieces for unit tests. */
 int  orc_link_q(int ip, double x0, double y0, double z0, double px, double py, double pz,
                 double radius_sq, double *q);
