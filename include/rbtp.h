@@ -314,8 +314,10 @@ int  rbtp_fp64_fma_rate(double *flops_per_s);
  * particle_state + c*npart), plane_sums (10*lx doubles, written).  It calls no allocator: its
  * partial sums live in one fixed device array of RBTP_NOALLOC_MAX_LX planes (2.6 MB per GPU, kept
  * until the process exits) whose address is looked up on the first call on each device, so make
- * that first call before any stream capture.  Calls share that array: calls that overlap on the GPU
- * race.  lx > RBTP_NOALLOC_MAX_LX returns RBTP_ERR_CAPACITY. */
+ * that first call before any stream capture; the address is kept for the device's primary context
+ * (the one the CUDA runtime uses), so it is stale after cudaDeviceReset.  Calls share that array:
+ * calls that overlap on the GPU race.  lx, ly, lz must be at least 3 (as rbtp_create requires;
+ * RBTP_ERR_ARG otherwise); lx > RBTP_NOALLOC_MAX_LX returns RBTP_ERR_CAPACITY. */
 #define RBTP_NOALLOC_MAX_LX 1024
 int  rbtp_plane_sums_noalloc(const double *ux, const double *uy, const double *uz, const double *phi,
                              const int *owner, const double *particle_state, int npart, int lx,

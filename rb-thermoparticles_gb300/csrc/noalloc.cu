@@ -6,14 +6,20 @@
 // allocations, or a latency-critical loop where the implicit device synchronisation of cudaMalloc
 // and cudaFree is not acceptable.  rbtp_plane_sums_noalloc serves them: the caller passes device
 // pointers to the fields and to the output, and the partial sums live in a fixed file-scope
-// device array (g_plane_scratch below, NOALLOC_CHUNKS x 10 x RBTP_NOALLOC_MAX_LX doubles =
-// 2.6 MB), which every GPU that loads this library holds until the process exits.
+// device array (g_plane_scratch below, NOALLOC_SLOTS x 10 doubles = 2.6 MB), which every GPU that
+// loads this library holds until the process exits.  The reduction itself is the handle's
+// (launch_plane_sums in diagnostics.cu, the same kernels), run with the fixed array as its
+// partial-sum buffer and as many row chunks as the array holds for the lattice's lx (at most the
+// handle's 512).
 //
 // The per-device address of that array is obtained once per device, on that device's first call,
 // with cudaGetSymbolAddress (host code cannot use the array's name as a device address).  Make the
-// first call on each device before any stream capture.  Every call shares the array: calls that
-// overlap on the GPU (different streams, or several host threads without ordering) race on it.
-// Each call writes every scratch element it later reads, so nothing needs clearing between calls.
+// first call on each device before any stream capture.  The cached address belongs to the device's
+// primary context as the CUDA runtime sets it up: after cudaDeviceReset, or with another driver
+// context current, it is stale.  Every call shares the array: calls that overlap on the GPU
+// (different streams, or several host threads without ordering) race on it.  Each call writes every
+// scratch element it later reads, so nothing needs clearing between calls.
+#include <algorithm>
 #include <mutex>
 
 #include "rbtp_internal.cuh"
@@ -21,72 +27,14 @@
 namespace rbtp {
 namespace {
 
-constexpr int NOALLOC_CHUNKS = 32;
-constexpr int NOALLOC_TX = 128;
+// (row chunk, plane) slots of ten partial sums each: 32 chunks of RBTP_NOALLOC_MAX_LX planes
+constexpr long long NOALLOC_SLOTS = 32LL * RBTP_NOALLOC_MAX_LX;
+constexpr int HANDLE_CHUNKS = 512;   // the handle's chunk count (rbtp_create)
 
-static __device__ __align__(256) double g_plane_scratch[NOALLOC_CHUNKS * NPLANEQ * RBTP_NOALLOC_MAX_LX];
+static __device__ __align__(256) double g_plane_scratch[NOALLOC_SLOTS * NPLANEQ];
 
 std::mutex g_scratch_mutex;
 double *g_scratch_ptr[256] = {};  // per device ordinal
-
-// Same ten per-plane quantities as the handle's reduction (diagnostics.cu).
-__global__ void __launch_bounds__(NOALLOC_TX) k_noalloc_partial(
-    int lx, int ly, int lz, double thot, double tcold, const double *ux, const double *uy,
-    const double *uz, const double *phi, const int *owner, const double *pst, int np,
-    double *scratch)
-{
-    const int ix = blockIdx.x * NOALLOC_TX + threadIdx.x;
-    const int chunk = blockIdx.y;
-    if (ix >= lx) return;
-    const long long lxy = (long long)lx * ly;
-    const long long rows = (long long)ly * lz;
-    const long long r0 = rows * chunk / NOALLOC_CHUNKS, r1 = rows * (chunk + 1) / NOALLOC_CHUNKS;
-    double q[NPLANEQ];
-#pragma unroll
-    for (int k = 0; k < NPLANEQ; ++k) q[k] = 0.0;
-    for (long long r = r0; r < r1; ++r) {
-        const int iz = (int)(r / ly);
-        const int iy = (int)(r - (long long)iz * ly);
-        const long long idx = (long long)iz * lxy + (long long)iy * lx + ix;
-        const double u = ux[idx], v = uy[idx], w = uz[idx], T = phi[idx];
-        const int own = owner ? owner[idx] : -1;
-        if (own < 0) {
-            q[0] += u * T;
-            q[1] += 1.0;
-            if (ix == 0) { q[4] += (thot - T) / 0.5; q[5] += 1.0; }
-            else if (ix == lx - 1) { q[4] += (T - tcold) / 0.5; q[5] += 1.0; }
-            q[6] += u; q[7] += v; q[8] += w; q[9] += T;
-        } else {
-            q[2] += u * T;
-            q[3] += 1.0;
-            if (own < np) {
-                const long long n = np;
-                const double relx = ((double)ix + 0.5) - pst[0 * n + own];
-                const double rely = ((double)iy + 0.5) - pst[1 * n + own];
-                const double relz = ((double)iz + 0.5) - pst[2 * n + own];
-                const double wx = pst[18 * n + own], wy = pst[19 * n + own], wz = pst[20 * n + own];
-                q[6] += pst[3 * n + own] + (relz * wy - rely * wz);
-                q[7] += pst[4 * n + own] + (relx * wz - relz * wx);
-                q[8] += pst[5 * n + own] + (rely * wx - relx * wy);
-                q[9] += pst[30 * n + own];
-            } else {
-                q[6] += u; q[7] += v; q[8] += w; q[9] += T;
-            }
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < NPLANEQ; ++k) scratch[((long long)chunk * NPLANEQ + k) * lx + ix] = q[k];
-}
-
-__global__ void k_noalloc_final(int lx, const double *scratch, double *plane)
-{
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= NPLANEQ * lx) return;
-    const int k = t / lx, ix = t - k * lx;
-    double s = 0.0;
-    for (int c = 0; c < NOALLOC_CHUNKS; ++c) s += scratch[((long long)c * NPLANEQ + k) * lx + ix];
-    plane[t] = s;
-}
 
 }  // namespace
 }  // namespace rbtp
@@ -99,7 +47,8 @@ extern "C" int rbtp_plane_sums_noalloc(const double *ux, const double *uy, const
 {
     using namespace rbtp;
     if (!ux || !uy || !uz || !phi || !plane_sums) return RBTP_ERR_ARG;
-    if (lx < 1 || ly < 1 || lz < 1 || npart < 0) return RBTP_ERR_ARG;
+    // the lattice sizes rbtp_create accepts (x = 0 and x = LX - 1 are distinct wall planes)
+    if (lx < 3 || ly < 3 || lz < 3 || npart < 0) return RBTP_ERR_ARG;
     if (lx > RBTP_NOALLOC_MAX_LX) return RBTP_ERR_CAPACITY;  // the scratch holds at most this many planes
     if (owner && npart > 0 && !particle_state) return RBTP_ERR_ARG;
     int dev = 0;
@@ -120,11 +69,20 @@ extern "C" int rbtp_plane_sums_noalloc(const double *ux, const double *uy, const
         }
         scratch = g_scratch_ptr[dev];
     }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const dim3 grd((lx + NOALLOC_TX - 1) / NOALLOC_TX, NOALLOC_CHUNKS, 1);
-    k_noalloc_partial<<<grd, NOALLOC_TX, 0, st>>>(lx, ly, lz, t_hot, t_cold, ux, uy, uz, phi,
-                                                  owner, particle_state, npart, scratch);
-    const int n = NPLANEQ * lx;
-    k_noalloc_final<<<(n + 255) / 256, 256, 0, st>>>(lx, scratch, plane_sums);
-    return cudaGetLastError() == cudaSuccess ? RBTP_OK : RBTP_ERR_CUDA;
+    Geo geo{};
+    geo.lx = lx; geo.ly = ly; geo.lz = lz;
+    geo.lxy = (long long)lx * ly;
+    geo.L = geo.lxy * lz;
+    Phys ph{};            // the plane sums read only the wall temperatures
+    ph.thot = t_hot;
+    ph.tcold = t_cold;
+    const long long rows = (long long)ly * lz;
+    const int nchunks = (int)std::min<long long>({rows, (long long)HANDLE_CHUNKS, NOALLOC_SLOTS / lx});
+    const cudaError_t e = launch_plane_sums(geo, ph, ux, uy, uz, phi, owner, particle_state, npart, scratch,
+                                            nchunks, plane_sums, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return RBTP_ERR_CUDA;
+    }
+    return RBTP_OK;
 }

@@ -39,11 +39,12 @@ def _nu_from_planes(pl, cfg, der):
 def _call(lib, torch, s, cfg):
     m = s.macros()
     dev = {k: torch.from_numpy(m[k]).cuda() for k in ("ux", "uy", "uz", "phi")}
-    owner = torch.from_numpy(s.flags()).cuda()
-    state = torch.from_numpy(np.ascontiguousarray(s.particles().T)).cuda()  # column-major
+    parts = s.npart > 0
+    owner = torch.from_numpy(s.flags()).cuda() if parts else None
+    state = torch.from_numpy(np.ascontiguousarray(s.particles().T)).cuda() if parts else None  # column-major
     out = torch.full((10 * cfg.lx,), float("nan"), dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream().cuda_stream
-    ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr())  # noqa: E731
     st = lib.rbtp_plane_sums_noalloc(ptr(dev["ux"]), ptr(dev["uy"]), ptr(dev["uz"]), ptr(dev["phi"]),
                                      ptr(owner), ptr(state), s.npart, cfg.lx, cfg.ly, cfg.lz,
                                      cfg.t_hot, cfg.t_cold, ptr(out), C.c_void_p(stream))
@@ -72,8 +73,32 @@ def test_noalloc_plane_sums_match_existing_entry_points(lib_built):
         assert np.allclose(means, s.means(), rtol=TOL, atol=1e-15)
 
 
+def test_noalloc_single_phase_ragged_planes(lib_built):
+    """No particles (owner and particle state NULL) and lx = 200, not a multiple of the reduction's
+    128-thread blocks; the x-profile too."""
+    torch = pytest.importorskip("torch")
+    lib = rbtp.load_library()
+    cfg = W.config("plain_fp64", lx=200, ly=24, lz=20)
+    der = rbtp.derive(cfg)
+    s = Solver(cfg)
+    s.load_state(*W.initial_state(cfg, seed=4, amp=1e-2))
+    for steps in (15, 4):
+        s.step(steps, macros_last=True)
+        pl = _call(lib, torch, s, cfg)
+        assert np.all(np.isfinite(pl))
+        row = np.array(s.nu(s.istep))
+        ours = _nu_from_planes(pl, cfg, der)
+        assert np.allclose(ours, row[[2, 3, 4, 5, 6]], rtol=TOL, atol=TOL), (ours, row)
+        assert np.allclose(pl[6:10].sum(axis=1) / cfg.nodes, s.means(), rtol=TOL, atol=1e-15)
+        prof = (pl[6:10] / (cfg.ly * cfg.lz)).T
+        assert np.allclose(prof, s.profile(), rtol=TOL, atol=1e-15)
+
+
 def test_noalloc_rejects_oversized_lattice(lib_built):
     lib = rbtp.load_library()
     d = C.c_void_p(16)  # never dereferenced: the size check comes first
     st = lib.rbtp_plane_sums_noalloc(d, d, d, d, None, None, 0, 4096, 8, 8, 1.0, 0.0, d, None)
     assert st == -8  # RBTP_ERR_CAPACITY
+    # lattices rbtp_create would reject (fewer than 3 nodes along an axis)
+    for dims in ((1, 8, 8), (8, 2, 8), (8, 8, 2)):
+        assert lib.rbtp_plane_sums_noalloc(d, d, d, d, None, None, 0, *dims, 1.0, 0.0, d, None) == -9
