@@ -148,7 +148,8 @@ int  rbtp_load_restart(rbtp_handle *h, const char *dir, int step);
 /* ---- time stepping ------------------------------------------------------------------------- */
 /* Advance nsteps full steps in main.cu:35-84 order (macrovar → forcing → collide/stream f →
  * IBB f → collide/stream g → IBB g → contacts → forces/heat → move → links → refill), fused into
- * one pull-stream/collide kernel per step plus the particle kernels.  Macroscopic fields are
+ * one stream/collide kernel per step on one in-place population array (AA pattern: even and odd
+ * steps alternate) plus the particle kernels.  Macroscopic fields are
  * materialised on steps that hit the config's
  * output cadence (NDIAG, NNUOUT, NFLOWOUT, NEND) and, with RBTP_STEP_MACROS_LAST, on the last
  * step of the call.  The dissipation fields ted/Ked of output_flow (compute_Ked/compute_ted,

@@ -185,7 +185,7 @@ int import_state(rbtp_handle *h, const double *f, const double *g, const double 
     const size_t P = 27 * (size_t)L * sizeof(double), F7 = 7 * (size_t)L * sizeof(double);
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-    void *fs = h->f[0], *gs = h->g[0];
+    void *fs = h->f, *gs = h->g;
     const double *df = static_cast<const double *>(device_view(h, f, P));
     const double *dg = static_cast<const double *>(device_view(h, g, P));
     const double *d7 = flow7 ? static_cast<const double *>(device_view(h, flow7, F7)) : nullptr;
@@ -322,7 +322,7 @@ int rbtp_footprint(const rbtp_config *cfg, size_t *bytes)
     const size_t L = (size_t)cfg->lx * cfg->ly * cfg->lz;
     const size_t P = 27 * L;
     const size_t sb = store_bytes(cfg->storage);
-    size_t b = 4 * P * sb;                                   // f, g double-buffered
+    size_t b = 2 * P * sb;                                   // f, g in place (AA storage)
     b += 8 * L * sizeof(double);                             // faux, rho, ux, uy, uz, phi, ted, ked
     b += 2 * (size_t)cfg->ly * cfg->lz * sizeof(double);     // rho_wall
     const size_t rows = (size_t)cfg->ly * cfg->lz;
@@ -402,15 +402,14 @@ int rbtp_create(const rbtp_config *cfg, rbtp_handle **out)
     }
     const size_t sb = store_bytes(h->mode);
     const size_t P = (size_t)27 * (size_t)L;
-    for (int k = 0; k < 2; ++k) {
-        if (h->mode == RBTP_STORE_F64) {
-            CKC(cudaMalloc(&h->f[k], P * sb));
-            CKC(cudaMalloc(&h->g[k], P * sb));
-        } else {
-            // paired (f_i, g_i) slots: f and g are the same allocation
-            CKC(cudaMalloc(&h->f[k], 2 * P * sb));
-            h->g[k] = h->f[k];
-        }
+    // one population array, updated in place (AA storage, rbtp_internal.cuh)
+    if (h->mode == RBTP_STORE_F64) {
+        CKC(cudaMalloc(&h->f, P * sb));
+        CKC(cudaMalloc(&h->g, P * sb));
+    } else {
+        // paired (f_i, g_i) slots: f and g are the same allocation
+        CKC(cudaMalloc(&h->f, 2 * P * sb));
+        h->g = h->f;
     }
     CKC(dalloc(&h->faux, L));
     CKC(dalloc(&h->rho_wall, 2 * (size_t)cfg->ly * cfg->lz));
@@ -483,11 +482,9 @@ int rbtp_destroy(rbtp_handle *h)
     rbtp_batch_detach(h);
     if (h->side) cudaStreamSynchronize(h->side);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    for (int k = 0; k < 2; ++k) {
-        if (h->g[k] != h->f[k]) cudaFree(h->g[k]);
-        cudaFree(h->f[k]);
-        cudaFree(h->owner[k]);
-    }
+    if (h->g != h->f) cudaFree(h->g);
+    cudaFree(h->f);
+    for (int k = 0; k < 2; ++k) cudaFree(h->owner[k]);
     cudaFree(h->faux); cudaFree(h->rho_wall);
     cudaFree(h->rho); cudaFree(h->ux); cudaFree(h->uy); cudaFree(h->uz); cudaFree(h->phi);
     cudaFree(h->ted); cudaFree(h->ked); cudaFree(h->fcol); cudaFree(h->gcol);
@@ -579,10 +576,9 @@ int rbtp_init_fresh(rbtp_handle *h)
         int s = upload_particles(h, rows.data());
         if (s) return s;
     }
-    CK(launch_fresh_init(h->mode, h->geo, h->ph, h->f[0], h->g[0], h->faux, h->rho, h->ux, h->uy,
+    CK(launch_fresh_init(h->mode, h->geo, h->ph, h->f, h->g, h->faux, h->rho, h->ux, h->uy,
                          h->uz, h->phi, h->stream));
     CK(cudaMemsetAsync(h->ted, 0, h->geo.L * sizeof(double), h->stream));
-    h->cur = 0;
     h->phase = PHASE_HOME;
     h->ocur = 0;
     CK(cudaMemsetAsync(h->status, 0, sizeof(DevStatus), h->stream));
@@ -607,7 +603,6 @@ int rbtp_load_state(rbtp_handle *h, const double *f, const double *g, const doub
     if (np > 0 && !particles) return fail(h, RBTP_ERR_ARG, "particle state required");
     int s = import_state(h, f, g, flow7);
     if (s) return s;
-    h->cur = 0;
     h->phase = PHASE_HOME;
     h->ocur = 0;
     CK(cudaMemsetAsync(h->status, 0, sizeof(DevStatus), h->stream));
@@ -648,13 +643,14 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
             s = ensure_scratch(h);
             if (s) return s;
         }
-        const int src = h->cur, dst = 1 - h->cur;
+        // AA storage: the step after a load or an odd step is even, the step after an even one odd
+        const bool odd = h->phase == PHASE_SWAPPED;
         StepBuffers b;
-        b.fin = h->f[src]; b.gin = h->g[src]; b.fout = h->f[dst]; b.gout = h->g[dst];
+        b.f = h->f; b.g = h->g;
         b.faux = h->faux; b.rho_wall = h->rho_wall;
         b.rho = h->rho; b.ux = h->ux; b.uy = h->uy; b.uz = h->uz; b.phi = h->phi;
         b.fcol = h->fcol; b.gcol = h->gcol; b.status = h->status;
-        CK(launch_step(h->mode, h->phase == PHASE_COLLIDED, out, h->geo, h->ph, b, h->stream));
+        CK(launch_step(h->mode, odd, out, h->geo, h->ph, b, h->stream));
         if (parts) {
             // Stream order: the contacts (positions only) run on the side stream beside IBB (both
             // latency-bound, few CTAs); the integrator waits for the contact forces.  The link
@@ -665,17 +661,16 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
             CK(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
             CK(launch_contacts(h->geo, h->ph, h->pb, h->status, h->side));
             CK(cudaEventRecord(h->ev_side, h->side));
-            CK(launch_links_ibb(h->mode, h->geo, h->ph, h->pb, h->f[dst], h->g[dst], h->rho, h->stream));
+            CK(launch_links_ibb(h->mode, h->geo, h->ph, h->pb, h->f, h->g, h->rho, odd, h->stream));
             CK(cudaStreamWaitEvent(h->stream, h->ev_side, 0));
             CK(launch_update(h->geo, h->ph, h->pb, h->stream));   // also refreshes the geometry cache
             s = build_links(h, on, true);
             if (s) return s;
-            CK(launch_refill(h->mode, h->geo, h->ph, h->pb, oc, on, h->f[dst], h->g[dst], h->faux,
-                             h->rho_wall, macro, h->rho, h->ux, h->uy, h->uz, h->phi, h->status, h->stream));
+            CK(launch_refill(h->mode, h->geo, h->ph, h->pb, oc, on, h->f, h->g, h->faux, h->rho_wall, macro,
+                             h->rho, h->ux, h->uy, h->uz, h->phi, h->status, odd, h->stream));
             h->ocur = 1 - h->ocur;
         }
-        h->cur = dst;
-        h->phase = PHASE_COLLIDED;
+        h->phase = odd ? PHASE_HOME : PHASE_SWAPPED;
         h->istep = istep;
         h->plane_valid = false;
         h->macros_valid = macro;
@@ -698,11 +693,10 @@ int rbtp_get_fg(rbtp_handle *h, double *f, double *g)
     if (s) return s;
     s = ensure_scratch(h);
     if (s) return s;
-    if (h->phase == PHASE_COLLIDED)
-        CK(launch_stream_export(h->mode, h->geo, h->ph, h->f[h->cur], h->g[h->cur], h->rho_wall, h->fcol,
-                                h->gcol, h->stream));
+    if (h->phase == PHASE_SWAPPED)
+        CK(launch_stream_export(h->mode, h->geo, h->ph, h->f, h->g, h->rho_wall, h->fcol, h->gcol, h->stream));
     else
-        CK(launch_home_export(h->mode, h->geo, h->ph, h->f[h->cur], h->g[h->cur], h->fcol, h->gcol, h->stream));
+        CK(launch_home_export(h->mode, h->geo, h->ph, h->f, h->g, h->fcol, h->gcol, h->stream));
     const size_t P = (size_t)27 * (size_t)h->geo.L;
     if (f) CK(cudaMemcpyAsync(f, h->fcol, P * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     if (g) CK(cudaMemcpyAsync(g, h->gcol, P * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1206,14 +1200,15 @@ int rbtp_load_restart(rbtp_handle *h, const char *dir, int step)
     return s;
 }
 
-// Exact checkpoint of a handle's whole step state in its storage precision: the populations as
-// they sit in the current buffer (post-collision with the IBB/refill fix-ups, or at home after a
-// load), the F_x auxiliary, the wall densities of the Dirichlet image, the macroscopic fields when
+// Exact checkpoint of a handle's whole step state in its storage precision: the population array as
+// it sits (post-streaming in the natural slots, or post-collision swapped with the IBB/refill
+// fix-ups, with the phase that says which), the F_x auxiliary, the wall densities of the Dirichlet image, the macroscopic fields when
 // they are current, and the 33 particle columns.  Solid flags and link slabs are rebuilt from the
 // positions on load (deterministically, as at the end of every step), so a run resumed from a
 // checkpoint continues bit for bit.  No counterpart in the reference.
 namespace {
 constexpr char CKP_MAGIC[9] = "RBTPCKP1";
+constexpr int CKP_VERSION = 2;   // 2: in-place AA population array
 struct CkpHeader {
     int version, mode, lx, ly, lz, np, phase, istep, macros_valid, pad;
 };
@@ -1227,7 +1222,8 @@ int rbtp_checkpoint_write(rbtp_handle *h, const char *path)
     if (!path) return fail(h, RBTP_ERR_ARG, "path is null");
     const size_t L = (size_t)h->geo.L, P = 27 * L * elem_bytes(h->mode), W = 2 * (size_t)h->geo.ly * h->geo.lz;
     const int np = h->pb.np;
-    CkpHeader hd{1, h->mode, h->geo.lx, h->geo.ly, h->geo.lz, np, h->phase, h->istep, h->macros_valid ? 1 : 0, 0};
+    CkpHeader hd{CKP_VERSION, h->mode, h->geo.lx, h->geo.ly, h->geo.lz, np, h->phase, h->istep,
+                 h->macros_valid ? 1 : 0, 0};
     std::vector<char> pop(P);
     std::vector<double> aux(L), wall(W), mac(h->macros_valid ? 5 * L : 0), prow((size_t)np * NP_COLS);
     CK(cudaStreamSynchronize(h->stream));
@@ -1236,10 +1232,10 @@ int rbtp_checkpoint_write(rbtp_handle *h, const char *path)
     bool ok = std::fwrite(CKP_MAGIC, 1, 8, fp) == 8 && std::fwrite(&hd, sizeof(hd), 1, fp) == 1 &&
               std::fwrite(&h->cfg, sizeof(rbtp_config), 1, fp) == 1;
     // 2P bytes of populations: f then g (FP64), or the paired (f_i, g_i) slots (float modes)
-    const bool paired = h->g[h->cur] == h->f[h->cur];
+    const bool paired = h->g == h->f;
     for (int k = 0; ok && k < 2; ++k) {
-        const char *src = paired ? static_cast<const char *>(h->f[h->cur]) + k * P
-                                 : static_cast<const char *>(k == 0 ? h->f[h->cur] : h->g[h->cur]);
+        const char *src = paired ? static_cast<const char *>(h->f) + k * P
+                                 : static_cast<const char *>(k == 0 ? h->f : h->g);
         if (cudaMemcpy(pop.data(), src, P, cudaMemcpyDeviceToHost) != cudaSuccess) {
             std::fclose(fp);
             return fail(h, RBTP_ERR_CUDA, "checkpoint read-back failed");
@@ -1282,9 +1278,14 @@ int rbtp_checkpoint_read(rbtp_handle *h, const char *path)
     rbtp_config saved;
     const bool head = std::fread(magic, 1, 8, fp) == 8 && std::memcmp(magic, CKP_MAGIC, 8) == 0 &&
                       std::fread(&hd, sizeof(hd), 1, fp) == 1 && std::fread(&saved, sizeof(saved), 1, fp) == 1;
-    if (!head || hd.version != 1) {
+    if (!head) {
         std::fclose(fp);
         return fail(h, RBTP_ERR_IO, std::string("not a checkpoint file: ") + path);
+    }
+    if (hd.version != CKP_VERSION) {
+        std::fclose(fp);
+        return fail(h, RBTP_ERR_IO, std::string("checkpoint format version ") + std::to_string(hd.version) +
+                                        " (this library reads version " + std::to_string(CKP_VERSION) + "): " + path);
     }
     if (hd.mode != h->mode || hd.lx != h->geo.lx || hd.ly != h->geo.ly || hd.lz != h->geo.lz || hd.np != h->pb.np) {
         std::fclose(fp);
@@ -1301,12 +1302,12 @@ int rbtp_checkpoint_read(rbtp_handle *h, const char *path)
                       std::fread(prow.data(), sizeof(double), prow.size(), fp) == prow.size();
     std::fclose(fp);
     if (!body) return fail(h, RBTP_ERR_IO, std::string("checkpoint is truncated: ") + path);
-    if (h->g[0] == h->f[0]) {   // paired (f_i, g_i) slots: the 2P bytes in file order
-        CK(cudaMemcpyAsync(h->f[0], f.data(), P, cudaMemcpyHostToDevice, h->stream));
-        CK(cudaMemcpyAsync(static_cast<char *>(h->f[0]) + P, g.data(), P, cudaMemcpyHostToDevice, h->stream));
+    if (h->g == h->f) {   // paired (f_i, g_i) slots: the 2P bytes in file order
+        CK(cudaMemcpyAsync(h->f, f.data(), P, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(static_cast<char *>(h->f) + P, g.data(), P, cudaMemcpyHostToDevice, h->stream));
     } else {
-        CK(cudaMemcpyAsync(h->f[0], f.data(), P, cudaMemcpyHostToDevice, h->stream));
-        CK(cudaMemcpyAsync(h->g[0], g.data(), P, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->f, f.data(), P, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->g, g.data(), P, cudaMemcpyHostToDevice, h->stream));
     }
     CK(cudaStreamSynchronize(h->stream));
     CK(aux_from_host(h, aux.data()));
@@ -1316,8 +1317,7 @@ int rbtp_checkpoint_read(rbtp_handle *h, const char *path)
         for (int k = 0; k < 5; ++k)
             CK(cudaMemcpyAsync(dst[k], &mac[k * L], L * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     }
-    h->cur = 0;
-    h->phase = hd.phase == PHASE_COLLIDED ? PHASE_COLLIDED : PHASE_HOME;
+    h->phase = hd.phase == PHASE_SWAPPED ? PHASE_SWAPPED : PHASE_HOME;
     h->ocur = 0;
     CK(cudaMemsetAsync(h->status, 0, sizeof(DevStatus), h->stream));
     h->ring_drained = 0;

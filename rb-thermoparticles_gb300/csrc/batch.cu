@@ -3,7 +3,7 @@
 // A batch advances many independent cavities in lockstep.  Per step it enqueues: a plan kernel
 // (each cavity's output mode for the step, from its cadence), ONE persistent launch of the fused
 // step over the packed tile table of all cavities, the particle pipeline as one launch per kernel
-// over the packed (cavity, particle) map, and an advance kernel (buffer/owner parity, phase, step
+// over the packed (cavity, particle) map, and an advance kernel (owner parity, AA phase, step
 // counter).  Every piece of per-step state lives in the device descriptors, so the sequence is
 // captured once into a CUDA graph and replayed for every step.  The autotuner times the candidate
 // (tile shape, persistent grid) pairs on the first steps of the batch — all candidates compute the
@@ -171,12 +171,14 @@ int refresh(rbtp_batch *b)
         std::memset(&d, 0, sizeof(d));
         d.geo = h->geo;
         d.ph = h->ph;
-        for (int k = 0; k < 2; ++k) { d.f[k] = h->f[k]; d.g[k] = h->g[k]; d.owner[k] = h->owner[k]; }
+        d.f = h->f;
+        d.g = h->g;
+        for (int k = 0; k < 2; ++k) d.owner[k] = h->owner[k];
         d.faux = h->faux; d.rho_wall = h->rho_wall;
         d.rho = h->rho; d.ux = h->ux; d.uy = h->uy; d.uz = h->uz; d.phi = h->phi;
         d.status = h->status;
         d.pb = h->pb;
-        d.cur = h->cur; d.ocur = h->ocur; d.phase = h->phase == PHASE_COLLIDED ? 1 : 0; d.istep = h->istep;
+        d.ocur = h->ocur; d.phase = h->phase; d.istep = h->istep;
         d.ndiag = h->cfg.ndiag; d.nnuout = h->cfg.nnuout; d.nflowout = h->cfg.nflowout; d.nend = h->cfg.nend;
         d.every = h->sample_every;
         d.mode = h->mode;
@@ -238,9 +240,8 @@ int sync_back(rbtp_batch *b)
     for (int m = 0; m < n; ++m) {
         rbtp_handle *h = b->members[m];
         const CavDesc &d = b->h_desc[m];
-        h->cur = d.cur;
         h->ocur = d.ocur;
-        h->phase = d.phase ? PHASE_COLLIDED : PHASE_HOME;
+        h->phase = d.phase == PHASE_SWAPPED ? PHASE_SWAPPED : PHASE_HOME;
         h->istep = d.istep;
         h->macros_valid = d.last_out == OUT_MACROS;
         h->dissip_valid = false;

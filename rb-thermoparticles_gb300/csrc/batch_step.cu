@@ -48,20 +48,19 @@ __global__ void k_batch_advance(CavDesc *desc, int n)
         CavDesc &d = desc[m];
         if (d.out == OUT_IDLE) continue;
         d.last_out = d.out;
-        d.cur ^= 1;
         if (d.pb.np > 0) d.ocur ^= 1;
-        d.phase = 1;
+        d.phase = d.phase == PHASE_SWAPPED ? PHASE_HOME : PHASE_SWAPPED;   // AA: even and odd alternate
         d.istep += 1;
     }
 }
 
-template <int MODE, bool PULL>
+template <int MODE, bool ODD>
 __device__ __forceinline__ void step_out(const Geo &geo, const Phys &ph, const StepBuffers &b, int out, int ix,
                                          int iy, int iz)
 {
-    if (out == OUT_NONE) step_node<MODE, PULL, OUT_NONE, false>(geo, ph, b, ix, iy, iz);
-    else if (out == OUT_RHO) step_node<MODE, PULL, OUT_RHO, false>(geo, ph, b, ix, iy, iz);
-    else step_node<MODE, PULL, OUT_MACROS, false>(geo, ph, b, ix, iy, iz);
+    if (out == OUT_NONE) step_node<MODE, ODD, OUT_NONE, false>(geo, ph, b, ix, iy, iz);
+    else if (out == OUT_RHO) step_node<MODE, ODD, OUT_RHO, false>(geo, ph, b, ix, iy, iz);
+    else step_node<MODE, ODD, OUT_MACROS, false>(geo, ph, b, ix, iy, iz);
 }
 
 // The batched kernel carries all phase/output variants of the step body behind block-uniform
@@ -94,18 +93,15 @@ __global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MI
         __syncthreads();
         const int ix = tl.y * TX + threadIdx.x, iy = tl.z * TY + threadIdx.y, iz = tl.w;
         if (d.out == OUT_IDLE || ix >= sgeo.lx || iy >= sgeo.ly) continue;
-        const int cur = d.cur;
         StepBuffers b;
-        b.fin = d.f[cur];
-        b.gin = d.g[cur];
-        b.fout = d.f[cur ^ 1];
-        b.gout = d.g[cur ^ 1];
+        b.f = d.f;
+        b.g = d.g;
         b.faux = d.faux;
         b.rho_wall = d.rho_wall;
         b.rho = d.rho; b.ux = d.ux; b.uy = d.uy; b.uz = d.uz; b.phi = d.phi;
         b.fcol = nullptr; b.gcol = nullptr;
         b.status = d.status;
-        if (d.phase) step_out<MODE, true>(sgeo, sph, b, d.out, ix, iy, iz);
+        if (d.phase == PHASE_SWAPPED) step_out<MODE, true>(sgeo, sph, b, d.out, ix, iy, iz);
         else step_out<MODE, false>(sgeo, sph, b, d.out, ix, iy, iz);
     }
 }

@@ -7,11 +7,6 @@
 
 #include "rbtp_internal.cuh"
 
-namespace rbtp {
-constexpr int PHASE_HOME = 0;      // current buffer holds post-streaming populations
-constexpr int PHASE_COLLIDED = 1;  // current buffer holds post-collision populations + fix-ups
-}  // namespace rbtp
-
 using namespace rbtp;
 
 struct rbtp_handle {
@@ -32,8 +27,7 @@ struct rbtp_handle {
     // particle steps: side stream for the contacts, which run beside IBB, with its fork/join events
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_side = nullptr;
-    void *f[2] = {nullptr, nullptr}, *g[2] = {nullptr, nullptr};
-    int cur = 0;
+    void *f = nullptr, *g = nullptr;    // the population array (g == f in the paired float modes)
     int phase = PHASE_HOME;
     double *faux = nullptr, *rho_wall = nullptr;
     double *rho = nullptr, *ux = nullptr, *uy = nullptr, *uz = nullptr, *phi = nullptr;

@@ -1,15 +1,17 @@
-// lbm_step.cu — fused D3Q27 f+g pull-stream / collide kernel for sm_103a.
+// lbm_step.cu — fused D3Q27 f+g stream/collide kernel (in-place AA storage) for sm_103a.
 //
 // One thread per lattice node.  The kernel replaces the reference's per-step sequence
 //   macrovar (macrovar.cu:3-34) -> forcing (macrovar.cu:36-47) -> collision_BGK (collision.cu:3-33)
 //   -> f_collide copy -> streaming (streaming.cu:3-23) -> collision_BGK_scalar (collision.cu:35-89)
 //   -> g_collide copy -> streaming_scalar (streaming.cu:25-63)
-// with a single read and a single write of every population.  The streaming of step n is
-// performed by the pull at the start of step n+1: the buffer written by step n holds the
-// post-collision populations f*(n) at their home node, and node x gathers f_i(x) = f*_i(x - c_i)
-// (or the wall bounce-back/Dirichlet image when x - c_i is outside the box).  Sparse particle
-// corrections (IBB, refill) are written by their own kernels into exactly the slots this gather
-// reads, so the bulk kernel never branches on solid flags.
+// with a single read and a single write of every population, in place: one population array in the
+// AA pattern (slots described in rbtp_internal.cuh).  Even steps read a node's post-streaming
+// populations from its natural slots and write the post-collision ones swapped into the same
+// node's slots; odd steps gather the swapped populations of the neighbours (streaming the even
+// step's output, with the wall bounce-back/Dirichlet image where x - c_i is outside the box) and
+// scatter their own output to the neighbours' natural slots (streaming it, walls applied at the
+// scatter).  Sparse particle corrections (IBB, refill) are written by their own kernels into exactly
+// the slots the next step reads, so the bulk kernel never branches on solid flags.
 //
 // The collision is the reference's BGK algebra regrouped by direction pairs (i, opp(i)): with
 // A = 4.5 (c.u)^2 - 1.5 u^2 (even in c) and B = 3 c.u (odd in c), both f and g post-collision
@@ -24,7 +26,7 @@ namespace rbtp {
 
 namespace {
 
-template <int MODE, bool PULL, int OUT>
+template <int MODE, bool ODD, int OUT>
 __global__ void __launch_bounds__(128, MODE == RBTP_STORE_F64 ? RBTP_STEP_MINB_F64 : RBTP_STEP_MINB_LOW)
     k_step(const Geo geo, const Phys ph, const StepBuffers b)
 {
@@ -34,11 +36,12 @@ __global__ void __launch_bounds__(128, MODE == RBTP_STORE_F64 ? RBTP_STEP_MINB_F
     const int iy = blockIdx.y * blockDim.y + threadIdx.y;
     const int iz = blockIdx.z;
     if (ix >= geo.lx || iy >= geo.ly) return;
-    step_node<MODE, PULL, OUT>(geo, ph, b, ix, iy, iz);
+    step_node<MODE, ODD, OUT>(geo, ph, b, ix, iy, iz);
 }
 
 // Stream-only export: the post-streaming populations f(n) of the reference (its d_f / d_g after a
-// step) reconstructed from the post-collision buffer, as FP64 home layout.
+// step) reconstructed from an array whose post-collision populations sit swapped (after an even
+// step): the odd step's gather without the collision, as FP64 home layout.
 template <int MODE>
 __global__ void __launch_bounds__(128) k_stream_export(const Geo geo, const Phys ph, const void *fin_,
                                                        const void *gin_, const double *rho_wall,
@@ -69,7 +72,8 @@ __global__ void __launch_bounds__(128) k_stream_export(const Geo geo, const Phys
         const bool oz = (cz == 1 && zlo) || (cz == -1 && zhi);
         const bool out = ox || oy || oz;
         const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
-        const long long src = out ? ((long long)o * L + node) : ((long long)i * L + node - off);
+        // f*_i(x - c_i) in slot (opp(i), x - c_i); outside the box f*_opp(i)(x) in slot (i, x)
+        const long long src = out ? ((long long)i * L + node) : ((long long)o * L + node - off);
         fout[(long long)i * L + node] = (double)ST::ld_f(fin + src, w, ph.t0);
         double gr = (double)ST::ld_g(gin + src, w, gshift(ph, out ? ix : ix - cx));
         if (ox && !oy && !oz) {
@@ -253,7 +257,7 @@ inline dim3 node_grid(const Geo &g, dim3 blk)
 inline unsigned lin_blocks(long long n, int t) { return (unsigned)((n + t - 1) / t); }
 
 template <int MODE>
-cudaError_t launch_step_mode(bool pull, int out, const Geo &geo, const Phys &ph,
+cudaError_t launch_step_mode(bool odd, int out, const Geo &geo, const Phys &ph,
                              const StepBuffers &b, cudaStream_t st)
 {
     // warps of 32 x-nodes in one row (FP64, FP32); 16 x 2 for shifted FP16, which is issue-bound:
@@ -262,7 +266,7 @@ cudaError_t launch_step_mode(bool pull, int out, const Geo &geo, const Phys &ph,
     const dim3 blk = MODE == RBTP_STORE_F16S ? dim3(16, 8, 1) : dim3(32, 4, 1);
     const dim3 grd = node_grid(geo, blk);
 #define RBTP_STEP_CASE(P, O)                                                       \
-    if (pull == P && out == O) return pdl_launch(k_step<MODE, P, O>, grd, blk, st, geo, ph, b);
+    if (odd == P && out == O) return pdl_launch(k_step<MODE, P, O>, grd, blk, st, geo, ph, b);
     RBTP_STEP_CASE(true, OUT_NONE)
     RBTP_STEP_CASE(true, OUT_RHO)
     RBTP_STEP_CASE(true, OUT_MACROS)
@@ -277,13 +281,13 @@ cudaError_t launch_step_mode(bool pull, int out, const Geo &geo, const Phys &ph,
 
 }  // namespace
 
-cudaError_t launch_step(int mode, bool pull, int out, const Geo &geo, const Phys &ph,
+cudaError_t launch_step(int mode, bool odd, int out, const Geo &geo, const Phys &ph,
                         const StepBuffers &b, cudaStream_t st)
 {
     switch (mode) {
-    case RBTP_STORE_F64: return launch_step_mode<RBTP_STORE_F64>(pull, out, geo, ph, b, st);
-    case RBTP_STORE_F32: return launch_step_mode<RBTP_STORE_F32>(pull, out, geo, ph, b, st);
-    case RBTP_STORE_F16S: return launch_step_mode<RBTP_STORE_F16S>(pull, out, geo, ph, b, st);
+    case RBTP_STORE_F64: return launch_step_mode<RBTP_STORE_F64>(odd, out, geo, ph, b, st);
+    case RBTP_STORE_F32: return launch_step_mode<RBTP_STORE_F32>(odd, out, geo, ph, b, st);
+    case RBTP_STORE_F16S: return launch_step_mode<RBTP_STORE_F16S>(odd, out, geo, ph, b, st);
     }
     return cudaErrorInvalidValue;
 }

@@ -8,7 +8,7 @@
 //     (node, direction) order, so the list is compact per particle and needs no global scan or
 //     host-side count (links.cu:50-139, 196-250);
 //   * IBB f/g, momentum exchange and heat flux: one CTA per particle walks its slab, writes the
-//     bounce-back values straight into the pull slots the next step reads, and reduces force,
+//     bounce-back values straight into the slots the next step reads, and reduces force,
 //     torque and heat with a fixed-order tree — deterministic, no floating-point atomics
 //     (ibb.cu:5-205);
 //   * contacts: a cell list; each particle sums its partners in ascending pid order, the order the
@@ -349,10 +349,41 @@ __device__ __forceinline__ void for_shell_nodes(ShellRows<NT> &sr, const Box &b,
 // ------------------------------------------------------------------------------------------------
 constexpr int IBB_THREADS = 128;
 
+// Slots of one link (x, ip) in the in-place AA storage after a step of the given parity: where the
+// post-collision populations f*_ip(x), f*_ip(x - c_ip) and f*_opp(x) sit, and the slot the next
+// step reads as f_opp(x), the population entering x from the solid node x + c_ip.  Even parity
+// (post-collision populations swapped into their own node's slots): (opp, x), (opp, x - c),
+// (ip, x) and (ip, x + c); odd parity (streamed to the neighbours' natural slots): (ip, x + c),
+// (ip, x), (opp, x - c) and (opp, x).  xs_* are the x-indices of the slots' nodes (the shift of
+// shifted-FP16 storage).  Reads touch only slots of fluid nodes and, in odd parity, the slot
+// (ip, x + c) of the solid node, which no link writes; writes touch slots of solid nodes (even)
+// or of fluid nodes that no link reads (odd), so reads and writes never alias.
+struct LinkSlots {
+    long long here, up, opp, out;
+    int xs_here, xs_up, xs_opp, xs_out;
+};
+__device__ __forceinline__ LinkSlots link_slots(bool odd, long long L, int ip, int o, long long x, long long x1,
+                                                long long solid, int ix, int cx)
+{
+    LinkSlots s;
+    if (odd) {
+        s.here = (long long)ip * L + solid; s.xs_here = ix + cx;
+        s.up = (long long)ip * L + x;       s.xs_up = ix;
+        s.opp = (long long)o * L + x1;      s.xs_opp = ix - cx;
+        s.out = (long long)o * L + x;       s.xs_out = ix;
+    } else {
+        s.here = (long long)o * L + x;      s.xs_here = ix;
+        s.up = (long long)o * L + x1;       s.xs_up = ix - cx;
+        s.opp = (long long)ip * L + x;      s.xs_opp = ix;
+        s.out = (long long)ip * L + solid;  s.xs_out = ix + cx;
+    }
+    return s;
+}
+
 template <int MODE>
 __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                                               void *f_, void *g_, const double *rho, int p, int chunk,
-                                               double *sh)
+                                               void *f_, void *g_, const double *rho, bool odd, int p,
+                                               int chunk, double *sh)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
@@ -395,17 +426,19 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             // upstream node x - c_ip, in-domain fluid (flag from the link build's owner reads)
             const bool fluid1 = (dw >> LINK_UP) & 1;
             const long long x1 = (long long)x - cxi - (long long)cyi * geo.lx - (long long)czi * geo.lxy;
+            const long long solid = (long long)x + cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
+            const LinkSlots sl = link_slots(odd, L, ip, o, x, x1, solid, ix, cxi);
 
-            const double f_here = fB[(long long)ip * L + x];
-            const double g_here = gB[(long long)ip * L + x];
+            const double f_here = fB[sl.here];
+            const double g_here = gB[sl.here];
             double fval, gval;
             // ibb.cu:52-73 (f: q < 0.5), ibb.cu:114-128 (g: q <= 0.5)
             if (fluid1) {
                 if (q < 0.5) {
-                    const double f_up = fB[(long long)ip * L + x1];
+                    const double f_up = fB[sl.up];
                     fval = 2.0 * q * f_here + (1.0 - 2.0 * q) * f_up - mom;
                 } else {
-                    const double f_oc = fB[(long long)o * L + x];
+                    const double f_oc = fB[sl.opp];
                     fval = (f_here - mom) * inv_2q + (2.0 * q - 1.0) * inv_2q * f_oc;
                 }
             } else {
@@ -414,20 +447,19 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const double amp = 2.0 * w * Tp * (1.0 + rho[x]);
             if (fluid1) {
                 if (q <= 0.5) {
-                    const double gu = gB[(long long)ip * L + x1];
+                    const double gu = gB[sl.up];
                     gval = -(2.0 * q * g_here + (1.0 - 2.0 * q) * gu) + amp;
                 } else {
-                    const double go = gB[(long long)o * L + x];
+                    const double go = gB[sl.opp];
                     gval = -g_here * inv_2q + amp * inv_2q + (2.0 * q - 1.0) * inv_2q * go;
                 }
             } else {
                 gval = -g_here + amp;
             }
-            // The population that streams into x along opp comes from the solid node x + c_ip: the
-            // pull of the next step reads it from slot (opp, x + c_ip).
-            const long long solid = (long long)x + cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
-            fB[(long long)o * L + solid] = fval;
-            gB[(long long)o * L + solid] = gval;
+            // the population that streams into x along opp from the solid node x + c_ip: the slot
+            // the next step reads as f_opp(x)
+            fB[sl.out] = fval;
+            gB[sl.out] = gval;
             // ibb.cu:160-187 (force, torque about the same intersection point) and 202-204 (heat)
             const double Fx = (cxi - uwx) * f_here - (-cxi - uwx) * fval;
             const double Fy = (cyi - uwy) * f_here - (-cyi - uwy) * fval;
@@ -481,36 +513,38 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             float q, f_here, g_here, f_2, g_2, rho;
             bool fluid1;
         };
+        auto slots_of = [&](int x, int ip) {
+            const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
+            const long long off = (long long)cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
+            return link_slots(odd, L, ip, dopp_rt(ip), x, (long long)x - off, (long long)x + off, x % geo.lx, cxi);
+        };
         auto gather = [&](int t, LinkIn &a) {
             a.x = __ldg(pb.link_node + base + t);
             const int dw = __ldg(pb.link_dir + base + t);
             a.ip = dw & LINK_DIR_MASK;
             a.q = (float)__ldg(pb.link_q + base + t);
             a.fluid1 = (dw >> LINK_UP) & 1;   // upstream node x - c_ip is in-domain fluid
-            const int ip = a.ip, x = a.x;
-            const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
-            const float wr = fweight_rt(ip);
-            const int ix = x % geo.lx;
-            ld2(fB + (long long)ip * L + x, ix, wr, a.f_here, a.g_here);
+            const float wr = fweight_rt(a.ip);
+            const LinkSlots sl = slots_of(a.x, a.ip);
+            ld2(fB + sl.here, sl.xs_here, wr, a.f_here, a.g_here);
             // ibb.cu:52-73 (f: q < 0.5) and ibb.cu:114-128 (g: q <= 0.5) interpolate with the
-            // upstream slot (ip, x - c_ip) below q = 1/2 and with the opposite slot (opp, x) above;
-            // at q = 1/2 f takes the opposite slot and g the upstream one (both are loaded)
+            // upstream population f*_ip(x - c_ip) below q = 1/2 and with the opposite f*_opp(x)
+            // above; at q = 1/2 f takes the opposite one and g the upstream one (both are loaded)
             a.f_2 = a.g_2 = 0.0f;
             if (a.fluid1) {
                 float fu, gu, fo, go;
                 if (a.q <= 0.5f) {
-                    const long long x1 = (long long)x - cxi - (long long)cyi * geo.lx - (long long)czi * geo.lxy;
-                    ld2(fB + (long long)ip * L + x1, ix - cxi, wr, fu, gu);
+                    ld2(fB + sl.up, sl.xs_up, wr, fu, gu);
                     a.f_2 = fu;
                     a.g_2 = gu;
                 }
                 if (a.q >= 0.5f) {
-                    ld2(fB + (long long)dopp_rt(ip) * L + x, ix, wr, fo, go);
+                    ld2(fB + sl.opp, sl.xs_opp, wr, fo, go);
                     a.f_2 = fo;
                     if (a.q > 0.5f) a.g_2 = go;
                 }
             }
-            a.rho = (float)__ldg(rho + x);
+            a.rho = (float)__ldg(rho + a.x);
         };
         auto finish = [&](const LinkIn &a) {
             const int x = a.x, ip = a.ip;
@@ -520,7 +554,6 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             const int iy = rem / geo.lx;
             const int ix = rem - iy * geo.lx;
             const int cxi = dcx_rt(ip), cyi = dcy_rt(ip), czi = dcz_rt(ip);
-            const int o = dopp_rt(ip);
             const float wr = fweight_rt(ip), winv = finvweight_rt(ip);   // w_opp = w_ip
             // moving wall velocity at the intersection point (ibb.cu:33-46)
             const float relx = ((float)(ix - ipx) + hx) + q * (float)cxi;
@@ -546,15 +579,15 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
             } else {
                 gval = -g_here + amp;
             }
-            // The population that streams into x along opp comes from the solid node x + c_ip: the
-            // pull of the next step reads it from slot (opp, x + c_ip).
-            const long long solid = (long long)x + cxi + (long long)cyi * geo.lx + (long long)czi * geo.lxy;
-            // one slot holds both populations (f and g buffers are the same allocation)
-            S *fs = fB + (long long)o * L + solid;
+            // the population that streams into x along opp from the solid node x + c_ip, in the slot
+            // the next step reads as f_opp(x); one slot holds both populations (f and g buffers
+            // are the same allocation)
+            const LinkSlots sl = slots_of(x, ip);
+            S *fs = fB + sl.out;
             float f_out = fval, g_out = gval;
             if constexpr (MODE == RBTP_STORE_F16S) {
                 // the value the reference would read back is the rounded one
-                const int ixs = ix + cxi;   // home of the written slot: the solid node
+                const int ixs = sl.xs_out;   // the node of the written slot
                 const __half2 hv = __floats2half2_rn(fval * winv, gval * winv - (tla + tlb * (float)ixs));
                 *fs = hv;
                 f_out = __low2float(hv) * wr;
@@ -608,10 +641,10 @@ __device__ __forceinline__ void links_ibb_body(const Geo &geo, const Phys &ph, c
 template <int MODE>
 __global__ void __launch_bounds__(IBB_THREADS, MODE == RBTP_STORE_F64 ? 4 : 6) k_links_ibb(const Geo geo, const Phys ph,
                                                            const PartBuffers pb, void *f_,
-                                                           void *g_, const double *rho)
+                                                           void *g_, const double *rho, bool odd)
 {
     __shared__ double sh[7 * IBB_THREADS];
-    links_ibb_body<MODE>(geo, ph, pb, f_, g_, rho, blockIdx.x, blockIdx.y, sh);
+    links_ibb_body<MODE>(geo, ph, pb, f_, g_, rho, odd, blockIdx.x, blockIdx.y, sh);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -1137,12 +1170,16 @@ __global__ void __launch_bounds__(NT) k_new_fluid(const Geo geo, const Phys ph, 
 }
 
 // Refill values (refill.cu:78-240): one warp per new-fluid node, lane ip computes population ip
-// from the post-collision populations of previous-step fluid neighbours (home slots of the
-// buffer just written by the step kernel).
+// from the post-collision populations f*_ip of previous-step fluid neighbours, as the step of the
+// given parity left them in the AA storage: after an even step in slot (opp(ip), n); after an odd
+// step in slot (ip, n + c_ip), or, where n + c_ip is outside the box, as the wall-processed
+// population in slot (opp(ip), n) (bounce-back: f*_ip itself; the Dirichlet image of g*_ip at a pure
+// x exit is inverted with the step's density at n, which the step kernel wrote to rho).
 template <int MODE>
 __device__ __forceinline__ void refill_compute_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
                                                     const int *owner_prev, const void *f_, const void *g_,
-                                                    const DevStatus *status, int warp0, int nwarps)
+                                                    const double *rho, bool odd, const DevStatus *status,
+                                                    int warp0, int nwarps)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
@@ -1167,6 +1204,28 @@ __device__ __forceinline__ void refill_compute_body(const Geo &geo, const Phys &
         if (lane < 27) {
             const int ip = lane;
             const double w = dweight_rt(ip);
+            const int cxp = dcx_rt(ip), cyp = dcy_rt(ip), czp = dcz_rt(ip), op = dopp_rt(ip);
+            // f*_ip and g*_ip of the previous-step fluid node n = (xn, yn, zn)
+            auto collided = [&](long long n, int xn, int yn, int zn, double &fo, double &go) {
+                if (!odd) {
+                    const long long sl = (long long)op * L + n;
+                    fo = (double)ST::ld_f(fB + sl, w, ph.t0);
+                    go = (double)ST::ld_g(gB + sl, w, gshift(ph, xn));
+                    return;
+                }
+                const int xd = xn + cxp, yd = yn + cyp, zd = zn + czp;
+                if (xd >= 0 && xd < geo.lx && yd >= 0 && yd < geo.ly && zd >= 0 && zd < geo.lz) {
+                    const long long sl = (long long)ip * L + (long long)zd * geo.lxy + (long long)yd * geo.lx + xd;
+                    fo = (double)ST::ld_f(fB + sl, w, ph.t0);
+                    go = (double)ST::ld_g(gB + sl, w, gshift(ph, xd));
+                    return;
+                }
+                const long long sl = (long long)op * L + n;
+                fo = (double)ST::ld_f(fB + sl, w, ph.t0);
+                go = (double)ST::ld_g(gB + sl, w, gshift(ph, xn));
+                const bool ox = xd < 0 || xd >= geo.lx, oyz = yd < 0 || yd >= geo.ly || zd < 0 || zd >= geo.lz;
+                if (ox && !oyz) go = wall_image(go, w, xd < 0 ? ph.thot : ph.tcold, rho[n]);
+            };
             double tf = 0.0, tg = 0.0;
             int sc = 0;
             for (int ip2 = 1; ip2 < 27; ++ip2) {
@@ -1177,13 +1236,15 @@ __device__ __forceinline__ void refill_compute_body(const Geo &geo, const Phys &
                 if (owner_prev[i1] >= 0) continue;
                 const int x2 = ix + 2 * cx2, y2 = iy + 2 * cy2, z2 = iz + 2 * cz2;
                 const bool in2 = x2 >= 0 && x2 < geo.lx && y2 >= 0 && y2 < geo.ly && z2 >= 0 && z2 < geo.lz;
-                const double f1 = (double)ST::ld_f(fB + (long long)ip * L + i1, w, ph.t0);
-                const double g1 = (double)ST::ld_g(gB + (long long)ip * L + i1, w, gshift(ph, x1));
+                double f1, g1;
+                collided(i1, x1, y1, z1, f1, g1);
                 if (in2) {
                     const long long i2 = (long long)z2 * geo.lxy + (long long)y2 * geo.lx + x2;
                     if (owner_prev[i2] < 0) {
-                        tf += 2.0 * f1 - (double)ST::ld_f(fB + (long long)ip * L + i2, w, ph.t0);
-                        tg += 2.0 * g1 - (double)ST::ld_g(gB + (long long)ip * L + i2, w, gshift(ph, x2));
+                        double f2, g2;
+                        collided(i2, x2, y2, z2, f2, g2);
+                        tf += 2.0 * f1 - f2;
+                        tg += 2.0 * g1 - g2;
                         ++sc;
                         continue;
                     }
@@ -1252,20 +1313,25 @@ __device__ __forceinline__ void refill_compute_body(const Geo &geo, const Phys &
 
 template <int MODE>
 __global__ void k_refill_compute(const Geo geo, const Phys ph, const PartBuffers pb,
-                                 const int *owner_prev, const void *f_, const void *g_,
-                                 const DevStatus *status)
+                                 const int *owner_prev, const void *f_, const void *g_, const double *rho,
+                                 bool odd, const DevStatus *status)
 {
-    refill_compute_body<MODE>(geo, ph, pb, owner_prev, f_, g_, status,
+    refill_compute_body<MODE>(geo, ph, pb, owner_prev, f_, g_, rho, odd, status,
                               (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
 }
 
-// Scatter the refill values into the slots the next pull reads at each new-fluid node.
+// Scatter the refill values, the post-streaming populations of each new-fluid node, into the
+// slots the next step reads: after an odd step the node's natural slots (the next, even, step reads
+// them as they are); after an even step the slots the next (odd) step gathers, (opp(ip), v - c_ip),
+// or, where v - c_ip is outside the box, (ip, v) holding the preimage of the wall rule the gather
+// applies.
 template <int MODE>
 __device__ __forceinline__ void refill_scatter_body(const Geo &geo, const Phys &ph, const PartBuffers &pb,
                                                     void *f_, void *g_, void *faux,
                                                     const double *rho_wall, bool macros, double *rho,
                                                     double *ux, double *uy, double *uz, double *phi,
-                                                    const DevStatus *status, long long t0, long long stride)
+                                                    const DevStatus *status, bool odd, long long t0,
+                                                    long long stride)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
@@ -1289,20 +1355,23 @@ __device__ __forceinline__ void refill_scatter_body(const Geo &geo, const Phys &
         const bool ox = (cx == 1 && ix == 0) || (cx == -1 && ix == geo.lx - 1);
         const bool oy = (cy == 1 && iy == 0) || (cy == -1 && iy == geo.ly - 1);
         const bool oz = (cz == 1 && iz == 0) || (cz == -1 && iz == geo.lz - 1);
-        if (!(ox || oy || oz)) {
+        if (odd) {
+            ST::st_f(fB + (long long)ip * L + idx, (R)fv, w, ph.t0);
+            ST::st_g(gB + (long long)ip * L + idx, (R)gv, w, gshift(ph, ix));
+        } else if (!(ox || oy || oz)) {
             const long long src = (long long)idx - cx - (long long)cy * geo.lx - (long long)cz * geo.lxy;
-            ST::st_f(fB + (long long)ip * L + src, (R)fv, w, ph.t0);
-            ST::st_g(gB + (long long)ip * L + src, (R)gv, w, gshift(ph, ix - cx));
+            ST::st_f(fB + (long long)o * L + src, (R)fv, w, ph.t0);
+            ST::st_g(gB + (long long)o * L + src, (R)gv, w, gshift(ph, ix - cx));
         } else {
-            ST::st_f(fB + (long long)o * L + idx, (R)fv, w, ph.t0);
+            ST::st_f(fB + (long long)ip * L + idx, (R)fv, w, ph.t0);
             double gs = gv;
             if (ox && !oy && !oz) {
-                // the pull applies g <- -stored + 2 w T_wall (1 + rho_wall); store its preimage
+                // the gather applies g <- -stored + 2 w T_wall (1 + rho_wall); store its preimage
                 const double tw = (cx == 1) ? ph.thot : ph.tcold;
                 const long long ws = (long long)iz * geo.ly + iy + (cx == 1 ? 0 : (long long)geo.lz * geo.ly);
                 gs = wall_image(gv, w, tw, rho_wall[ws]);
             }
-            ST::st_g(gB + (long long)o * L + idx, (R)gs, w, gshift(ph, ix));
+            ST::st_g(gB + (long long)ip * L + idx, (R)gs, w, gshift(ph, ix));
         }
         if (ip == 0) {
             static_cast<typename Store<MODE>::A *>(faux)[idx] = 0;
@@ -1318,9 +1387,9 @@ template <int MODE>
 __global__ void k_refill_scatter(const Geo geo, const Phys ph, const PartBuffers pb, void *f_,
                                  void *g_, void *faux, const double *rho_wall, bool macros,
                                  double *rho, double *ux, double *uy, double *uz, double *phi,
-                                 const DevStatus *status)
+                                 const DevStatus *status, bool odd)
 {
-    refill_scatter_body<MODE>(geo, ph, pb, f_, g_, faux, rho_wall, macros, rho, ux, uy, uz, phi, status,
+    refill_scatter_body<MODE>(geo, ph, pb, f_, g_, faux, rho_wall, macros, rho, ux, uy, uz, phi, status, odd,
                               (long long)blockIdx.x * blockDim.x + threadIdx.x,
                               (long long)gridDim.x * blockDim.x);
 }
@@ -1336,10 +1405,10 @@ __global__ void k_refill_scatter(const Geo geo, const Phys ph, const PartBuffers
     }
 
 cudaError_t launch_links_ibb(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                             void *f, void *g, const double *rho, cudaStream_t st)
+                             void *f, void *g, const double *rho, bool odd, cudaStream_t st)
 {
     if (pb.np <= 0) return cudaSuccess;
-    RBTP_MODE_DISPATCH(mode, (k_links_ibb<M><<<dim3(pb.np, pb.ibb_chunks), IBB_THREADS, 0, st>>>(geo, ph, pb, f, g, rho)));
+    RBTP_MODE_DISPATCH(mode, (k_links_ibb<M><<<dim3(pb.np, pb.ibb_chunks), IBB_THREADS, 0, st>>>(geo, ph, pb, f, g, rho, odd)));
     return cudaGetLastError();
 }
 
@@ -1398,7 +1467,7 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
                           const int *owner_prev, const int *owner_cur, void *f, void *g,
                           void *faux, const double *rho_wall, bool macros, double *rho,
                           double *ux, double *uy, double *uz, double *phi, DevStatus *status,
-                          cudaStream_t st)
+                          bool odd, cudaStream_t st)
 {
     if (pb.np <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(&status->nf_count, 0, sizeof(int), st);
@@ -1407,16 +1476,17 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
         k_new_fluid<LINK_WIDE><<<pb.np, LINK_WIDE, 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
     else
         k_new_fluid<LINK_NARROW><<<pb.np, LINK_NARROW, 0, st>>>(geo, ph, pb, owner_prev, owner_cur, status);
-    RBTP_MODE_DISPATCH(mode, (k_refill_compute<M><<<152, 256, 0, st>>>(geo, ph, pb, owner_prev, f, g, status)));
-    RBTP_MODE_DISPATCH(mode, (k_refill_scatter<M><<<152, 256, 0, st>>>(geo, ph, pb, f, g, faux, rho_wall, macros, rho, ux, uy, uz, phi, status)));
+    RBTP_MODE_DISPATCH(mode, (k_refill_compute<M><<<152, 256, 0, st>>>(geo, ph, pb, owner_prev, f, g, rho, odd, status)));
+    RBTP_MODE_DISPATCH(mode, (k_refill_scatter<M><<<152, 256, 0, st>>>(geo, ph, pb, f, g, faux, rho_wall, macros, rho, ux, uy, uz, phi, status, odd)));
     return cudaGetLastError();
 }
 
 // =================================================================================================
 // Batched particle pipeline: the same per-particle bodies, with (cavity, particle) taken from a
-// packed particle map and each cavity's buffers and step state from its device descriptor.  The
-// populations of the current step are in buffer cur ^ 1 (the step kernel wrote them), the solid
-// flags of the previous build in owner[ocur] and the new ones go to owner[ocur ^ 1].
+// packed particle map and each cavity's buffers and step state from its device descriptor.  They
+// run after the step kernel and before the advance kernel: the parity of the step just taken is
+// the descriptor's phase (PHASE_SWAPPED: odd), the solid flags of the previous build are in
+// owner[ocur] and the new ones go to owner[ocur ^ 1].
 // =================================================================================================
 namespace {
 
@@ -1430,8 +1500,7 @@ __global__ void __launch_bounds__(IBB_THREADS, MODE == RBTP_STORE_F64 ? 4 : 6) k
     const int2 mp = pmap[cm.x];
     const CavDesc &d = desc[mp.x];
     if (d.out == OUT_IDLE) return;
-    const int w = d.cur ^ 1;
-    links_ibb_body<MODE>(d.geo, d.ph, d.pb, d.f[w], d.g[w], d.rho, mp.y, cm.y, sh);
+    links_ibb_body<MODE>(d.geo, d.ph, d.pb, d.f, d.g, d.rho, d.phase == PHASE_SWAPPED, mp.y, cm.y, sh);
 }
 
 __global__ void k_cells_zero_b(const CavDesc *desc, const int *pmem)
@@ -1567,9 +1636,9 @@ __global__ void k_refill_compute_b(const CavDesc *desc, const int *pmem)
     pdl_trigger();
     const CavDesc &d = desc[pmem[blockIdx.y]];
     if (d.out == OUT_IDLE) return;
-    const int w = d.cur ^ 1;
-    refill_compute_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f[w], d.g[w], d.status,
-                              (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5);
+    refill_compute_body<MODE>(d.geo, d.ph, d.pb, d.owner[d.ocur], d.f, d.g, d.rho, d.phase == PHASE_SWAPPED,
+                              d.status, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                              (gridDim.x * blockDim.x) >> 5);
 }
 
 template <int MODE>
@@ -1579,9 +1648,8 @@ __global__ void k_refill_scatter_b(const CavDesc *desc, const int *pmem)
     pdl_trigger();
     const CavDesc &d = desc[pmem[blockIdx.y]];
     if (d.out == OUT_IDLE) return;
-    const int w = d.cur ^ 1;
-    refill_scatter_body<MODE>(d.geo, d.ph, d.pb, d.f[w], d.g[w], d.faux, d.rho_wall, d.out == OUT_MACROS,
-                              d.rho, d.ux, d.uy, d.uz, d.phi, d.status,
+    refill_scatter_body<MODE>(d.geo, d.ph, d.pb, d.f, d.g, d.faux, d.rho_wall, d.out == OUT_MACROS,
+                              d.rho, d.ux, d.uy, d.uz, d.phi, d.status, d.phase == PHASE_SWAPPED,
                               (long long)blockIdx.x * blockDim.x + threadIdx.x,
                               (long long)gridDim.x * blockDim.x);
 }

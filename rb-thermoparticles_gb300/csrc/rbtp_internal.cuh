@@ -276,9 +276,26 @@ enum StepOut { OUT_NONE = 0, OUT_RHO = 1, OUT_MACROS = 2, OUT_MACROS_COL = 3, OU
 // ------------------------------------------------------------------------------------------------
 // Kernel launch wrappers (defined in the .cu files).
 // ------------------------------------------------------------------------------------------------
+// In-place AA storage.  One array holds every population slot (i, x) (direction-major, [ip][z][y][x]);
+// steps alternate between two kinds, so that each slot is read and written by the same thread:
+//   even step (natural -> swapped): node x reads its post-streaming f_i(x) from slot (i, x) and
+//     writes its post-collision f*_i(x) to slot (opp(i), x);
+//   odd step (swapped -> natural): node x gathers f_i(x) = f*_i(x - c_i) from slot
+//     (opp(i), x - c_i), or, where x - c_i is outside the box, the wall's image of f*_opp(i)(x)
+//     from slot (i, x); it writes f*_i(x) to slot (i, x + c_i), or, where x + c_i is outside, the
+//     wall-processed population f_opp(i)(x) of the next step to slot (opp(i), x).
+// Node x of an odd step reads exactly the slots it writes, so one array serves both halves.  The
+// streaming of an even step's output happens in the next odd step's gather (which applies the walls
+// with the even step's wall densities, rho_wall); the streaming of an odd step's output happens in
+// its own scatter (walls applied with the node's own density).  After an odd step the natural slots
+// hold post-streaming populations (PHASE_HOME), after an even step the post-collision populations
+// of every node sit swapped in its own slots (PHASE_SWAPPED).  Shifted-FP16 storage keeps each slot
+// relative to the conduction profile at the slot's own node.
+constexpr int PHASE_HOME = 0;      // natural slots hold post-streaming populations: the next step is even
+constexpr int PHASE_SWAPPED = 1;   // post-collision populations (+ IBB/refill fix-ups) stored swapped:
+                                   // the next step is odd
 struct StepBuffers {
-    const void *fin, *gin;
-    void *fout, *gout;
+    void *f, *g;        // the population array (g == f in the paired float modes), read and written
     void *faux;         // F_x of the previous step in, F_x of this step out (L of Store<MODE>::A)
     double *rho_wall;   // density deviation at the x = 0 and x = LX-1 planes (2*LY*LZ)
     double *rho, *ux, *uy, *uz, *phi;   // macro outputs (L each), may be null
@@ -286,8 +303,10 @@ struct StepBuffers {
     DevStatus *status;
 };
 
-cudaError_t launch_step(int mode, bool pull, int out, const Geo &geo, const Phys &ph,
+cudaError_t launch_step(int mode, bool odd, int out, const Geo &geo, const Phys &ph,
                         const StepBuffers &b, cudaStream_t st);
+// Post-streaming populations f(n) (the reference's d_f / d_g after a step) from an array in
+// PHASE_SWAPPED, as FP64 home layout: the odd step's gather, walls included, without collision.
 cudaError_t launch_stream_export(int mode, const Geo &geo, const Phys &ph, const void *fin,
                                  const void *gin, const double *rho_wall, double *fout,
                                  double *gout, cudaStream_t st);
@@ -364,8 +383,10 @@ struct PartBuffers {
     int box_half_mark, box_half_link, box_half_nf;
 };
 
+// IBB after a step of the given parity (odd: the step just taken was odd; slots as StepBuffers
+// describes).
 cudaError_t launch_links_ibb(int mode, const Geo &geo, const Phys &ph, const PartBuffers &pb,
-                             void *f, void *g, const double *rho, cudaStream_t st);
+                             void *f, void *g, const double *rho, bool odd, cudaStream_t st);
 cudaError_t launch_contacts(const Geo &geo, const Phys &ph, const PartBuffers &pb,
                             DevStatus *status, cudaStream_t st);
 // The integrator also refreshes the particles' geometry cache (PGeo) for their new positions.
@@ -379,7 +400,7 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
                           const int *owner_prev, const int *owner_cur, void *f, void *g,
                           void *faux, const double *rho_wall, bool macros, double *rho,
                           double *ux, double *uy, double *uz, double *phi, DevStatus *status,
-                          cudaStream_t st);
+                          bool odd, cudaStream_t st);
 
 // ------------------------------------------------------------------------------------------------
 // Batched execution: one descriptor per cavity in device memory.  The step state (buffer parity,
@@ -389,13 +410,13 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
 struct CavDesc {
     Geo geo;
     Phys ph;
-    void *f[2], *g[2];
+    void *f, *g;                        // the population array (in-place AA storage)
     void *faux;                         // F_x auxiliary (Store<MODE>::A)
     double *rho_wall, *rho, *ux, *uy, *uz, *phi;
     DevStatus *status;
     PartBuffers pb;
     int *owner[2];
-    int cur, ocur, phase, istep;        // advanced on the device
+    int ocur, phase, istep;             // advanced on the device (phase: PHASE_HOME / PHASE_SWAPPED)
     int ndiag, nnuout, nflowout, nend;  // output cadence (<= 0: never)
     int every;                          // extra macro cadence (sampling), <= 0: never
     int out;                            // this step's output mode (written by the plan kernel)

@@ -1,5 +1,5 @@
-// step_node.cuh — the per-node body of the fused pull-stream/collide step (see lbm_step.cu for the
-// algorithm and its reference mapping).  Included by lbm_step.cu (single cavity) and batch_step.cu
+// step_node.cuh — the per-node body of the fused stream/collide step on the in-place AA storage
+// (see lbm_step.cu for the algorithm and its reference mapping, rbtp_internal.cuh for the slots).  Included by lbm_step.cu (single cavity) and batch_step.cu
 // (many cavities over a packed tile table), which instantiate it for their launch shapes.
 #pragma once
 
@@ -18,13 +18,16 @@
 
 namespace rbtp {
 
-// One node of the fused step; shared by the single-cavity kernel below and the batched kernel of
-// batch.cu.  (ix, iy, iz) must lie inside the lattice.  INTERIOR_PATH adds a second copy of the
-// gather without the box-face tests, taken by warps none of whose nodes touches a face.  It pays
-// only where the step is issue-bound (shifted-FP16 storage: -11 % instructions, -11 % time at
-// 320x320x160); FP32 is HBM-bound and FP64 FP64-pipe-bound, and the batched kernel (six step
-// variants in one kernel, small cavities whose warps nearly all touch an x face) leaves it out.
-template <int MODE, bool PULL, int OUT, bool INTERIOR_PATH = true>
+// One node of the fused step in the in-place AA storage (StepBuffers describes the slots); shared
+// by the single-cavity kernel (lbm_step.cu) and the batched kernel (batch_step.cu).  (ix, iy, iz)
+// must lie inside the lattice.  ODD selects the odd step (gather from swapped neighbour slots,
+// scatter to natural neighbour slots, walls at both ends); the even step reads and writes the
+// node's own slots only.  INTERIOR_PATH adds, for odd steps, a second copy of the gather and the
+// scatter without the box-face tests, taken by warps none of whose nodes touches a face.  It pays
+// only where the step is issue-bound (shifted-FP16 storage: -11 % instructions at 320x320x160);
+// FP32 is HBM-bound and FP64 FP64-pipe-bound, and the batched kernel (six step variants in one
+// kernel, small cavities whose warps nearly all touch an x face) leaves it out.
+template <int MODE, bool ODD, int OUT, bool INTERIOR_PATH = true>
 __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const StepBuffers &b, int ix,
                                           int iy, int iz)
 {
@@ -33,10 +36,9 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     using R = typename ST::R;
     const long long L = geo.L;
     const long long node = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
-    const S *__restrict__ fin = static_cast<const S *>(b.fin);
-    const S *__restrict__ gin = static_cast<const S *>(b.gin);
-    S *__restrict__ fout = static_cast<S *>(b.fout);
-    S *__restrict__ gout = static_cast<S *>(b.gout);
+    // read and written in place: no restrict (the paired float modes alias f and g)
+    S *fA = static_cast<S *>(b.f);
+    S *gA = static_cast<S *>(b.g);
     const double t0 = ph.t0;
     const bool xlo = ix == 0, xhi = ix == geo.lx - 1;
     const bool ylo = iy == 0, yhi = iy == geo.ly - 1;
@@ -45,10 +47,10 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     const StepK<R> &K = step_consts<R>(ph);
 
     // Shifted-FP16 storage works in its scaled variables throughout: F_i = f_i / w_i and
-    // G_i = g_i / w_i - T_c(x_home) are what the memory holds (T_c the conduction profile at the
-    // slot's home node), the moments take the weights once per lattice-weight class, and the
+    // G_i = g_i / w_i - T_c(x_slot) are what the memory holds (T_c the conduction profile at the
+    // slot's own node), the moments take the weights once per lattice-weight class, and the
     // collision constants are divided by w_i (no per-population scaling on load or store).  A
-    // pulled G_i is relative to s_i = T_c(x - c_ix) = Tc - tlb c_ix, a linear function of c_ix, so
+    // gathered G_i is relative to s_i = T_c(x - c_ix) = Tc - tlb c_ix, a linear function of c_ix, so
     // its moment and collision corrections are closed-form.  The other modes work on f_i and g_i.
     constexpr bool SC = MODE == RBTP_STORE_F16S;
     const R Tc = SC ? K.tla + K.tlb * (R)ix : (R)0;   // T_c at this node
@@ -68,56 +70,60 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     using A = typename ST::A;
     const A fold_in = __ldg(static_cast<const A *>(b.faux) + node);
     R f[27], g[27];
-    // INTERIOR: no neighbour of this warp's nodes leaves the box, so every pull is the plain
-    // f*_i(x - c_i) (the face tests and the bounce-back selects drop out)
+    // INTERIOR: no neighbour of this warp's nodes leaves the box, so every odd-step gather is the
+    // plain f*_i(x - c_i) and every scatter the plain slot (i, x + c_i) (the face tests and the
+    // wall selects drop out)
     auto gather = [&](auto INT) {
         constexpr bool INTERIOR = decltype(INT)::value;
         unroll<27>([&](auto I) {
             constexpr int i = decltype(I)::value;
             constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i), o = dopp(i);
             constexpr double w = dweight(i);
-            if constexpr (!PULL || i == 0) {
+            if constexpr (!ODD || i == 0) {
+                // even step: the post-streaming f_i(x) in the natural slot (i, x)
                 if constexpr (ST::PAIRED) {
-                    ldfg(fin + (long long)i * L + node, w, f[i], g[i]);
+                    ldfg(fA + (long long)i * L + node, w, f[i], g[i]);
                 } else {
-                    f[i] = ST::ld_f(fin + (long long)i * L + node, w, t0);
-                    g[i] = ST::ld_g(gin + (long long)i * L + node, w, t0);
+                    f[i] = ST::ld_f(fA + (long long)i * L + node, w, t0);
+                    g[i] = ST::ld_g(gA + (long long)i * L + node, w, t0);
                 }
             } else {
-                // f_i(x) = f*_i(x - c_i); a neighbour outside the box returns f*_opp(x) (bounce-back)
+                // odd step: f_i(x) = f*_i(x - c_i), swapped into slot (opp(i), x - c_i); a
+                // neighbour outside the box returns f*_opp(i)(x), swapped into slot (i, x)
                 const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
-                long long src = (long long)i * L + node - off;
+                long long src = (long long)o * L + node - off;
                 if constexpr (!INTERIOR) {
                     const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
                                      (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
                     if constexpr (SC) {
-                        if (out) src = (long long)o * L + node;
+                        if (out) src = (long long)i * L + node;
                     } else {
-                        src = out ? ((long long)o * L + node) : src;
+                        src = out ? ((long long)i * L + node) : src;
                     }
                 }
                 if constexpr (ST::PAIRED) {
-                    ldfg(fin + src, w, f[i], g[i]);
+                    ldfg(fA + src, w, f[i], g[i]);
                 } else {
-                    f[i] = ST::ld_f(fin + src, w, t0);
-                    g[i] = ST::ld_g(gin + src, w, t0);
+                    f[i] = ST::ld_f(fA + src, w, t0);
+                    g[i] = ST::ld_g(gA + src, w, t0);
                 }
             }
         });
     };
     const bool face = xlo || xhi || ylo || yhi || zlo || zhi;
-    if (INTERIOR_PATH && SC && PULL && !__any_sync(__activemask(), face)) gather(std::true_type{});
+    const bool interior = INTERIOR_PATH && SC && ODD && !__any_sync(__activemask(), face);
+    if (interior) gather(std::true_type{});
     else gather(std::false_type{});
-    if constexpr (!PULL && SC) {
-        // home slots (first step after a load): every G_i is relative to T_c(x), not s_i
+    if constexpr (!ODD && SC) {
+        // natural slots: every G_i is relative to T_c(x), not s_i
         unroll<27>([&](auto I) {
             constexpr int i = decltype(I)::value;
             constexpr int cx = dcx(i);
             if constexpr (cx != 0) g[i] += K.tlb * (R)cx;
         });
     }
-    if constexpr (PULL && SC) {
-        // a bounce-back slot's home is this node: re-express its G relative to s_i (one branch
+    if constexpr (ODD && SC) {
+        // a bounce-back slot belongs to this node: re-express its G relative to s_i (one branch
         // around the whole correction, taken only by box-surface nodes)
         if (xlo || xhi || ylo || yhi || zlo || zhi) {
             unroll<27>([&](auto I) {
@@ -131,10 +137,11 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
             });
         }
     }
-    if constexpr (PULL) {
-        // streaming.cu:45-61: at the x walls a direction that leaves only through x takes the
-        // Dirichlet anti-bounce-back with the node's density deviation of the previous step; y/z
-        // exits stay adiabatic.  Only warps holding x-wall nodes enter this branch.
+    if constexpr (ODD) {
+        // streaming.cu:45-61 for the even step's output: at the x walls a direction that leaves
+        // only through x takes the Dirichlet anti-bounce-back with the node's density deviation of
+        // the (even) step that produced it; y/z exits stay adiabatic.  Only warps holding x-wall
+        // nodes enter this branch.
         if (xlo || xhi) {
             const R rw = (R)b.rho_wall[(xhi ? (long long)geo.lz * geo.ly : 0) + wall_slot];
             const R tw = xlo ? K.thot : K.tcold;
@@ -159,8 +166,12 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     }
 
     // ---- moments (macrovar.cu:3-34), pairwise ----
-    R rho = f[0], jx = 0, jy = 0, jz = 0;
-    R phi = g[0], kx = 0, ky = 0, kz = 0;
+    // Sums start from -0.0: -0.0 + x == x for every x, so the compiler drops the first addition
+    // (it may not fold +0.0 + x, which differs for x = -0.0); only the sign of an exact zero can
+    // differ from a +0.0 start.
+    constexpr R NZ = -(R)0;
+    R rho = f[0], jx = NZ, jy = NZ, jz = NZ;
+    R phi = g[0], kx = NZ, ky = NZ, kz = NZ;
     if constexpr (SC) {
         // per weight class: sums of the scaled variables, then one multiply by the class weight
         rho = (R)dweight(0) * f[0];
@@ -168,7 +179,7 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
         kx = -K.tlb * (R)(1.0 / 3.0);        // sum_i c_i w_i s_i = -tlb sum_i w_i c_i c_ix
         unroll<3>([&](auto C) {
             constexpr int c = decltype(C)::value + 1;
-            R r_ = 0, p_ = 0, ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+            R r_ = NZ, p_ = NZ, ax = NZ, ay = NZ, az = NZ, bx = NZ, by = NZ, bz = NZ;
             unroll<13>([&](auto Kp) {
                 constexpr int i = dpair(decltype(Kp)::value);
                 if constexpr (dclass(i) == c) {
@@ -226,8 +237,11 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     } else if constexpr (OUT == OUT_RHO) {
         b.rho[node] = (double)rho;
     }
-    if (xlo) b.rho_wall[wall_slot] = (double)rho;
-    if (xhi) b.rho_wall[(long long)geo.lz * geo.ly + wall_slot] = (double)rho;
+    if constexpr (!ODD) {
+        // the wall densities the next (odd) step's gather and the stream export apply
+        if (xlo) b.rho_wall[wall_slot] = (double)rho;
+        if (xhi) b.rho_wall[(long long)geo.lz * geo.ly + wall_slot] = (double)rho;
+    }
 
     // ---- f collision (collision.cu:3-33) ----
     // f*_i = om f_i + w_i [ (rho + P_i)/tau + G (c_ix - u_x)(1 + P_i) ],  P_i = A_i + B_i,
@@ -282,7 +296,7 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
             if constexpr (dclass(i) == c) {
                 constexpr int o = dopp(i);
                 constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
-                R cu = 0, cV = 0;
+                R cu = NZ, cV = NZ;
                 if constexpr (cx != 0) { cu += (R)cx * ux; cV += (R)cx * vx; }
                 if constexpr (cy != 0) { cu += (R)cy * uy; cV += (R)cy * vy; }
                 if constexpr (cz != 0) { cu += (R)cz * uz; cV += (R)cz * vz; }
@@ -305,28 +319,71 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
         });
     });
 
-    unroll<27>([&](auto I) {
-        constexpr int i = decltype(I)::value;
-        constexpr double w = dweight(i);
+    // store one slot: fv, gv in the working variables (shifted FP16: gv relative to T_c of the
+    // slot's own node)
+    auto put = [&](long long slot, R fv, R gv, double w) {
         if constexpr (SC) {
-            fout[(long long)i * L + node] = __floats2half2_rn(f[i], g[i]);
-            if constexpr (OUT == OUT_MACROS_COL) {
-                b.fcol[(long long)i * L + node] = (double)((R)w * f[i]);
-                b.gcol[(long long)i * L + node] = (double)((R)w * (g[i] + Tc));
-            }
+            fA[slot] = __floats2half2_rn(fv, gv);
+        } else if constexpr (ST::PAIRED) {
+            fA[slot] = make_float2(fv, gv);
         } else {
-            if constexpr (ST::PAIRED) {
-                fout[(long long)i * L + node] = make_float2(f[i], g[i]);
+            ST::st_f(fA + slot, fv, w, t0);
+            ST::st_g(gA + slot, gv, w, t0);
+        }
+    };
+    auto scatter = [&](auto INT) {
+        constexpr bool INTERIOR = decltype(INT)::value;
+        unroll<27>([&](auto I) {
+            constexpr int i = decltype(I)::value;
+            constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i), o = dopp(i);
+            constexpr double w = dweight(i);
+            if constexpr (!ODD || i == 0) {
+                // even step: f*_i(x) swapped into the node's own slot (opp(i), x)
+                put((long long)o * L + node, f[i], g[i], w);
             } else {
-                ST::st_f(fout + (long long)i * L + node, f[i], w, t0);
-                ST::st_g(gout + (long long)i * L + node, g[i], w, t0);
+                // odd step: f*_i(x) streams to slot (i, x + c_i); a population leaving the box
+                // becomes the next step's f_opp(i)(x) in slot (opp(i), x): bounce-back for f, and
+                // for g adiabatic at y/z exits or the Dirichlet image -g* + 2 w T_wall (1 + rho)
+                // with this node's density at a pure x exit (streaming.cu:3-63)
+                bool out = false;
+                if constexpr (!INTERIOR)
+                    out = (cx == 1 && xhi) || (cx == -1 && xlo) || (cy == 1 && yhi) || (cy == -1 && ylo) ||
+                          (cz == 1 && zhi) || (cz == -1 && zlo);
+                if (!out) {
+                    const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
+                    // shifted FP16: relative to T_c(x + c_i) = T_c(x) + tlb c_ix
+                    put((long long)i * L + node + off, f[i], SC ? g[i] - K.tlb * (R)cx : g[i], w);
+                } else {
+                    R gv = g[i];
+                    if constexpr (cx != 0) {
+                        const bool ox = (cx == 1) ? xhi : xlo;
+                        const bool oyz = (cy == 1 && yhi) || (cy == -1 && ylo) || (cz == 1 && zhi) || (cz == -1 && zlo);
+                        if (ox && !oyz) {
+                            const R tw = (cx == -1) ? K.thot : K.tcold;
+                            if constexpr (SC) {
+                                const R wi = (R)w;
+                                gv = wall_image(wi * (g[i] + Tc), w, tw, rho) * (R)(1.0 / w) - Tc;
+                            } else {
+                                gv = wall_image(g[i], w, tw, rho);
+                            }
+                        }
+                    }
+                    put((long long)o * L + node, f[i], gv, w);
+                }
             }
             if constexpr (OUT == OUT_MACROS_COL) {
-                b.fcol[(long long)i * L + node] = (double)f[i];
-                b.gcol[(long long)i * L + node] = (double)g[i];
+                if constexpr (SC) {
+                    b.fcol[(long long)i * L + node] = (double)((R)w * f[i]);
+                    b.gcol[(long long)i * L + node] = (double)((R)w * (g[i] + Tc));
+                } else {
+                    b.fcol[(long long)i * L + node] = (double)f[i];
+                    b.gcol[(long long)i * L + node] = (double)g[i];
+                }
             }
-        }
-    });
+        });
+    };
+    if (interior) scatter(std::true_type{});
+    else scatter(std::false_type{});
 }
 
 }  // namespace rbtp

@@ -75,13 +75,15 @@ def test_workload_configs():
 
 def test_footprint_covers_the_population_buffers(lib_built):
     """rbtp_footprint (the server's admission size) is host arithmetic: for every storage mode it
-    covers the two population buffers (27 L paired (f, g) slots each, FP64 keeps separate f and g
-    arrays), orders the modes by their bytes, and grows with particles."""
+    covers the one in-place population array (27 L paired (f, g) slots, FP64 keeps separate f and
+    g arrays) and not a second copy of it, orders the modes by their bytes, and grows with
+    particles."""
     from rbtp import footprint
     L = 320 * 320 * 160
-    pop = {0: 2 * 2 * 27 * L * 8, 1: 2 * 27 * L * 8, 2: 2 * 27 * L * 4}
+    pop = {0: 2 * 27 * L * 8, 1: 27 * L * 8, 2: 27 * L * 4}
     fp = {st: footprint(W.config("production", storage=st)) for st in (0, 1, 2)}
     for st in (0, 1, 2):
         assert pop[st] <= fp[st] < pop[st] + 16 * 8 * L     # plus at most 16 FP64 fields per node
+        assert fp[st] < 2 * pop[st] or st == 2               # no second population buffer
     assert fp[0] > fp[1] > fp[2]
     assert footprint(W.config("particle_laden", storage=1)) > fp[1]
