@@ -27,8 +27,8 @@ namespace rbtp {
 namespace {
 
 template <int MODE, bool ODD, int OUT>
-__global__ void __launch_bounds__(128, MODE == RBTP_STORE_F64 ? RBTP_STEP_MINB_F64 : RBTP_STEP_MINB_LOW)
-    k_step(const Geo geo, const Phys ph, const StepBuffers b)
+__global__ void __launch_bounds__(128, RBTP_STEP_MINB(MODE))
+    k_step(const Geo geo, const Phys ph, const StepBuffers b, const AAOff ao)
 {
     pdl_wait();
     pdl_trigger();
@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(128, MODE == RBTP_STORE_F64 ? RBTP_STEP_MINB_F
     const int iy = blockIdx.y * blockDim.y + threadIdx.y;
     const int iz = blockIdx.z;
     if (ix >= geo.lx || iy >= geo.ly) return;
-    step_node<MODE, ODD, OUT>(geo, ph, b, ix, iy, iz);
+    step_node<MODE, ODD, OUT>(geo, ph, b, ao, ix, iy, iz);
 }
 
 // Stream-only export: the post-streaming populations f(n) of the reference (its d_f / d_g after a
@@ -260,13 +260,17 @@ template <int MODE>
 cudaError_t launch_step_mode(bool odd, int out, const Geo &geo, const Phys &ph,
                              const StepBuffers &b, cudaStream_t st)
 {
-    // warps of 32 x-nodes in one row (FP64, FP32); 16 x 2 for shifted FP16, which is issue-bound:
-    // half as many warps hold an x-face node and take the bounce-back gather (-1.4 % time at
-    // 320x320x160; FP32, HBM-bound, is 1.7 % slower with it)
-    const dim3 blk = MODE == RBTP_STORE_F16S ? dim3(16, 8, 1) : dim3(32, 4, 1);
+    // Warps of 32 x-nodes in one row (FP64, FP32: 16-wide blocks cost 3 % at 320x320x160, wider
+    // ones nothing).  Shifted FP16 is issue-bound: its odd steps use 16 x 2 warps, so that half as
+    // many warps hold an x-face node and take the face-tested gather and scatter (0.717 against
+    // 0.729 ms for 32-wide blocks at 320x320x160); its even steps, which touch no neighbour, run
+    // best in 64-node rows (0.574 against 0.606 ms for 16 x 8 blocks).
+    dim3 blk(32, 4, 1);
+    if (MODE == RBTP_STORE_F16S) blk = odd ? dim3(16, 8, 1) : (geo.lx % 64 == 0 ? dim3(64, 2, 1) : dim3(32, 4, 1));
     const dim3 grd = node_grid(geo, blk);
+    const AAOff ao = make_aa_off(geo);
 #define RBTP_STEP_CASE(P, O)                                                       \
-    if (odd == P && out == O) return pdl_launch(k_step<MODE, P, O>, grd, blk, st, geo, ph, b);
+    if (odd == P && out == O) return pdl_launch(k_step<MODE, P, O>, grd, blk, st, geo, ph, b, ao);
     RBTP_STEP_CASE(true, OUT_NONE)
     RBTP_STEP_CASE(true, OUT_RHO)
     RBTP_STEP_CASE(true, OUT_MACROS)

@@ -204,6 +204,22 @@ struct Geo {
     long long lxy, L;
 };
 
+// Slot offsets of the odd (swapped -> natural) step relative to a node's own slot of direction 0,
+// in elements: the gather of direction i reads slot (opp i, x - c_i) at g[i] = opp(i) L - off_i,
+// and the scatter of direction i writes slot (i, x + c_i) at i L + off_i = g[opp i]
+// (off_i = c_ix + c_iy LX + c_iz LX LY).  Built once per launch on the host, so the kernel takes
+// each offset from its parameters instead of forming it in every warp.
+struct AAOff {
+    long long g[27];
+};
+inline AAOff make_aa_off(const Geo &geo)
+{
+    AAOff a;
+    for (int i = 0; i < 27; ++i)
+        a.g[i] = (long long)dopp(i) * geo.L - ((long long)dcx(i) + (long long)dcy(i) * geo.lx + (long long)dcz(i) * geo.lxy);
+    return a;
+}
+
 // Relaxation and forcing constants of the step kernel, precomputed on the host in the kernel's
 // arithmetic type (per-thread double divisions would occupy GB300's narrow FP64 pipe).
 template <class R>

@@ -8,15 +8,52 @@
 #include "rbtp_internal.cuh"
 
 // Resident 128-thread blocks per SM requested from the register allocator (FP64 is bound by the
-// FP64 pipe, the FP32/FP16 storage modes by HBM bandwidth).
+// FP64 pipe, FP32 storage by HBM bandwidth, shifted-FP16 storage by instruction issue).  Best of
+// 4/5/6 sweeps of both step parities at 320x320x160 on GB300: 5 (<= 96 registers) for FP32 and
+// shifted FP16.  At 6 (<= 80 registers) the FP32 steps are 5 % slower and the shifted-FP16 even
+// step, spilling, takes twice as long.
 #ifndef RBTP_STEP_MINB_F64
 #define RBTP_STEP_MINB_F64 1
 #endif
-#ifndef RBTP_STEP_MINB_LOW
-#define RBTP_STEP_MINB_LOW 6  // 6 x 128 threads (<= 80 registers): best of a 1/5/6/8 sweep on GB300
+#ifndef RBTP_STEP_MINB_F32
+#define RBTP_STEP_MINB_F32 5
 #endif
+#ifndef RBTP_STEP_MINB_F16S
+#define RBTP_STEP_MINB_F16S 5
+#endif
+#define RBTP_STEP_MINB(MODE)                                                 \
+    ((MODE) == RBTP_STORE_F64 ? RBTP_STEP_MINB_F64                           \
+                              : ((MODE) == RBTP_STORE_F32 ? RBTP_STEP_MINB_F32 : RBTP_STEP_MINB_F16S))
 
 namespace rbtp {
+
+// (f_i, g_i) of one direction held as one value.  The moments and both collisions apply the same
+// operation to f and to g, pair by pair, so in the float modes the pair is a float2 and sm_100's
+// packed FP32x2 instructions (FADD2, FMUL2, FFMA2: IEEE single operations on both halves, round
+// to nearest) advance both halves in one issue slot.  FP64 keeps two scalar operations.
+template <typename R>
+struct PairOps;
+template <>
+struct PairOps<float> {
+    using T = float2;
+    static __device__ __forceinline__ T mk(float a, float b) { return make_float2(a, b); }
+    static __device__ __forceinline__ T add(T a, T b) { return __fadd2_rn(a, b); }
+    static __device__ __forceinline__ T sub(T a, T b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+    static __device__ __forceinline__ T mul(T a, T b) { return __fmul2_rn(a, b); }
+    static __device__ __forceinline__ T fma(T a, T b, T c) { return __ffma2_rn(a, b, c); }
+};
+template <>
+struct PairOps<double> {
+    using T = double2;
+    static __device__ __forceinline__ T mk(double a, double b) { return make_double2(a, b); }
+    static __device__ __forceinline__ T add(T a, T b) { return make_double2(a.x + b.x, a.y + b.y); }
+    static __device__ __forceinline__ T sub(T a, T b) { return make_double2(a.x - b.x, a.y - b.y); }
+    static __device__ __forceinline__ T mul(T a, T b) { return make_double2(a.x * b.x, a.y * b.y); }
+    static __device__ __forceinline__ T fma(T a, T b, T c)
+    {
+        return make_double2(__fma_rn(a.x, b.x, c.x), __fma_rn(a.y, b.y, c.y));
+    }
+};
 
 // One node of the fused step in the in-place AA storage (StepBuffers describes the slots); shared
 // by the single-cavity kernel (lbm_step.cu) and the batched kernel (batch_step.cu).  (ix, iy, iz)
@@ -27,9 +64,18 @@ namespace rbtp {
 // only where the step is issue-bound (shifted-FP16 storage: -11 % instructions at 320x320x160);
 // FP32 is HBM-bound and FP64 FP64-pipe-bound, and the batched kernel (six step variants in one
 // kernel, small cavities whose warps nearly all touch an x face) leaves it out.
-template <int MODE, bool ODD, int OUT, bool INTERIOR_PATH = true>
-__device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const StepBuffers &b, int ix,
-                                          int iy, int iz)
+//
+// FRESH_SCATTER: the scatter addresses its slots from an opaque copy of the node index.  A node
+// writes exactly the slots it read (both parities), so otherwise the compiler keeps the gather's
+// addresses (two registers each) live across the collision rather than recompute them.  Where
+// the lattice sizes are per-thread values (the batched kernel stages them in shared memory) that
+// spilled 400-480 bytes per thread at 128 registers and the copy removes every spill (+7 % ensemble
+// throughput); with shifted FP16 it takes the odd step from 0.748 to 0.717 ms at 320x320x160.  FP32
+// gains nothing and FP64 (255 registers) loses half its speed, so they leave it out.
+template <int MODE, bool ODD, int OUT, bool INTERIOR_PATH = true, bool FRESH_SCATTER = MODE == RBTP_STORE_F16S && ODD,
+          bool HAS_OFF = true>
+__device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const StepBuffers &b, const AAOff &ao,
+                                          int ix, int iy, int iz)
 {
     using ST = Store<MODE>;
     using S = typename ST::S;
@@ -37,8 +83,25 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     const long long L = geo.L;
     const long long node = (long long)iz * geo.lxy + (long long)iy * geo.lx + ix;
     // read and written in place: no restrict (the paired float modes alias f and g)
-    S *fA = static_cast<S *>(b.f);
-    S *gA = static_cast<S *>(b.g);
+    S *const fA = static_cast<S *>(b.f);
+    S *const gA = static_cast<S *>(b.g);
+    // Every slot a node touches is its own slot of direction 0 plus a kernel-uniform offset: i L
+    // (its own slot i), o L - off_i (odd gather), i L + off_i (odd scatter).  Addressed as one
+    // per-thread base pointer plus that offset, the offset stays in the load or store instruction;
+    // written as (o L + node) - off_i, each access cost two 64-bit integer additions (odd steps ran
+    // 1.6-2x the even steps' instructions).
+    const S *const fN = fA + node;
+    const S *const gN = gA + node;
+    // the odd step's gather offset of direction I (AAOff): from the launch parameters, or formed
+    // from the lattice sizes where the caller has no table (the batched kernel)
+    auto aa_gather = [&](auto I) -> long long {
+        constexpr int i = decltype(I)::value;
+        if constexpr (HAS_OFF) {
+            return ao.g[i];
+        } else {
+            return (long long)dopp(i) * L - ((long long)dcx(i) + (long long)dcy(i) * geo.lx + (long long)dcz(i) * geo.lxy);
+        }
+    };
     const double t0 = ph.t0;
     const bool xlo = ix == 0, xhi = ix == geo.lx - 1;
     const bool ylo = iy == 0, yhi = iy == geo.ly - 1;
@@ -54,22 +117,25 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     // its moment and collision corrections are closed-form.  The other modes work on f_i and g_i.
     constexpr bool SC = MODE == RBTP_STORE_F16S;
     const R Tc = SC ? K.tla + K.tlb * (R)ix : (R)0;   // T_c at this node
+    // (f_i, g_i) of one direction as one pair value (PairOps): a float2 in the float modes
+    using PO = PairOps<R>;
+    using V = typename PO::T;
+    constexpr R NZ = -(R)0;
+    constexpr V NZ2 = V{NZ, NZ};
     // both populations of a slot (one access in the paired layouts of the float modes)
-    auto ldfg = [&](const S *p, double w, R &fv, R &gv) {
+    auto ldfg = [&](const S *pf, const S *pg, double w) -> V {
         if constexpr (SC) {
-            const __half2 v = *p;
-            fv = __low2float(v);
-            gv = __high2float(v);
+            return __half22float2(*pf);
         } else if constexpr (ST::PAIRED) {
-            const float2 v = *p;
-            fv = v.x;
-            gv = v.y;
+            return *pf;
+        } else {
+            return PO::mk(ST::ld_f(pf, w, t0), ST::ld_g(pg, w, t0));
         }
     };
     // F_x of the previous step, read ahead of the population gather
     using A = typename ST::A;
     const A fold_in = __ldg(static_cast<const A *>(b.faux) + node);
-    R f[27], g[27];
+    V fg[27];
     // INTERIOR: no neighbour of this warp's nodes leaves the box, so every odd-step gather is the
     // plain f*_i(x - c_i) and every scatter the plain slot (i, x + c_i) (the face tests and the
     // wall selects drop out)
@@ -81,32 +147,21 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
             constexpr double w = dweight(i);
             if constexpr (!ODD || i == 0) {
                 // even step: the post-streaming f_i(x) in the natural slot (i, x)
-                if constexpr (ST::PAIRED) {
-                    ldfg(fA + (long long)i * L + node, w, f[i], g[i]);
-                } else {
-                    f[i] = ST::ld_f(fA + (long long)i * L + node, w, t0);
-                    g[i] = ST::ld_g(gA + (long long)i * L + node, w, t0);
-                }
+                fg[i] = ldfg(fN + (long long)i * L, gN + (long long)i * L, w);
             } else {
                 // odd step: f_i(x) = f*_i(x - c_i), swapped into slot (opp(i), x - c_i); a
                 // neighbour outside the box returns f*_opp(i)(x), swapped into slot (i, x)
-                const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
-                long long src = (long long)o * L + node - off;
+                long long src = aa_gather(I);
                 if constexpr (!INTERIOR) {
                     const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
                                      (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
                     if constexpr (SC) {
-                        if (out) src = (long long)i * L + node;
+                        if (out) src = (long long)i * L;
                     } else {
-                        src = out ? ((long long)i * L + node) : src;
+                        src = out ? (long long)i * L : src;
                     }
                 }
-                if constexpr (ST::PAIRED) {
-                    ldfg(fA + src, w, f[i], g[i]);
-                } else {
-                    f[i] = ST::ld_f(fA + src, w, t0);
-                    g[i] = ST::ld_g(gA + src, w, t0);
-                }
+                fg[i] = ldfg(fN + src, gN + src, w);
             }
         });
     };
@@ -119,7 +174,7 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
         unroll<27>([&](auto I) {
             constexpr int i = decltype(I)::value;
             constexpr int cx = dcx(i);
-            if constexpr (cx != 0) g[i] += K.tlb * (R)cx;
+            if constexpr (cx != 0) fg[i].y += K.tlb * (R)cx;
         });
     }
     if constexpr (ODD && SC) {
@@ -132,7 +187,7 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
                 if constexpr (i != 0 && cx != 0) {
                     const bool out = (cx == 1 && xlo) || (cx == -1 && xhi) || (cy == 1 && ylo) ||
                                      (cy == -1 && yhi) || (cz == 1 && zlo) || (cz == -1 && zhi);
-                    if (out) g[i] += K.tlb * (R)cx;
+                    if (out) fg[i].y += K.tlb * (R)cx;
                 }
             });
         }
@@ -155,9 +210,9 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
                         if constexpr (SC) {
                             const R wi = (R)dweight(i);
                             const R si = Tc - K.tlb * (R)cx;
-                            g[i] = wall_image(wi * (g[i] + si), dweight(i), tw, rw) * (R)(1.0 / dweight(i)) - si;
+                            fg[i].y = wall_image(wi * (fg[i].y + si), dweight(i), tw, rw) * (R)(1.0 / dweight(i)) - si;
                         } else {
-                            g[i] = wall_image(g[i], dweight(i), tw, rw);
+                            fg[i].y = wall_image(fg[i].y, dweight(i), tw, rw);
                         }
                     }
                 }
@@ -165,61 +220,50 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
         }
     }
 
-    // ---- moments (macrovar.cu:3-34), pairwise ----
-    // Sums start from -0.0: -0.0 + x == x for every x, so the compiler drops the first addition
-    // (it may not fold +0.0 + x, which differs for x = -0.0); only the sign of an exact zero can
+    // ---- moments (macrovar.cu:3-34), pairwise, f and g together ----
+    // m0 = (rho, phi), mx = (j_x, k_x) = (sum_i c_ix f_i, sum_i c_ix g_i), my, mz likewise.  Sums
+    // start from -0.0: -0.0 + x == x for every x, so the compiler drops the first addition (it
+    // may not fold +0.0 + x, which differs for x = -0.0); only the sign of an exact zero can
     // differ from a +0.0 start.
-    constexpr R NZ = -(R)0;
-    R rho = f[0], jx = NZ, jy = NZ, jz = NZ;
-    R phi = g[0], kx = NZ, ky = NZ, kz = NZ;
+    V m0 = fg[0], mx = NZ2, my = NZ2, mz = NZ2;
+    auto pair_moments = [&](auto Kp, V &s0, V &sx, V &sy, V &sz) {
+        constexpr int i = dpair(decltype(Kp)::value);
+        constexpr int o = dopp(i);
+        constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+        const V sum = PO::add(fg[i], fg[o]), dif = PO::sub(fg[i], fg[o]);
+        s0 = PO::add(s0, sum);
+        if constexpr (cx == 1) sx = PO::add(sx, dif);
+        if constexpr (cx == -1) sx = PO::sub(sx, dif);
+        if constexpr (cy == 1) sy = PO::add(sy, dif);
+        if constexpr (cy == -1) sy = PO::sub(sy, dif);
+        if constexpr (cz == 1) sz = PO::add(sz, dif);
+        if constexpr (cz == -1) sz = PO::sub(sz, dif);
+    };
     if constexpr (SC) {
-        // per weight class: sums of the scaled variables, then one multiply by the class weight
-        rho = (R)dweight(0) * f[0];
-        phi = (R)dweight(0) * g[0] + Tc;     // sum_i w_i (G_i + s_i), sum_i w_i s_i = T_c
-        kx = -K.tlb * (R)(1.0 / 3.0);        // sum_i c_i w_i s_i = -tlb sum_i w_i c_i c_ix
+        // per weight class: sums of the scaled variables, then one multiply by the class weight;
+        // rho = w_0 F_0 + ..., phi = w_0 G_0 + T_c + ... (sum_i w_i s_i = T_c), and
+        // k_x starts at sum_i c_ix w_i s_i = -tlb sum_i w_i c_ix^2 = -tlb / 3
+        m0 = PO::fma(PO::mk((R)dweight(0), (R)dweight(0)), fg[0], PO::mk(NZ, Tc));
+        mx = PO::mk(NZ, -K.tlb * (R)(1.0 / 3.0));
         unroll<3>([&](auto C) {
             constexpr int c = decltype(C)::value + 1;
-            R r_ = NZ, p_ = NZ, ax = NZ, ay = NZ, az = NZ, bx = NZ, by = NZ, bz = NZ;
+            V s0 = NZ2, sx = NZ2, sy = NZ2, sz = NZ2;
             unroll<13>([&](auto Kp) {
-                constexpr int i = dpair(decltype(Kp)::value);
-                if constexpr (dclass(i) == c) {
-                    constexpr int o = dopp(i);
-                    constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
-                    const R sf = f[i] + f[o], df = f[i] - f[o];
-                    const R sg = g[i] + g[o], dg = g[i] - g[o];
-                    r_ += sf;
-                    p_ += sg;
-                    if constexpr (cx == 1) { ax += df; bx += dg; }
-                    if constexpr (cx == -1) { ax -= df; bx -= dg; }
-                    if constexpr (cy == 1) { ay += df; by += dg; }
-                    if constexpr (cy == -1) { ay -= df; by -= dg; }
-                    if constexpr (cz == 1) { az += df; bz += dg; }
-                    if constexpr (cz == -1) { az -= df; bz -= dg; }
-                }
+                if constexpr (dclass(dpair(decltype(Kp)::value)) == c) pair_moments(Kp, s0, sx, sy, sz);
             });
             constexpr R w = (R)(c == 1 ? 2.0 / 27.0 : (c == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
-            rho += w * r_;
-            phi += w * p_;
-            jx += w * ax; jy += w * ay; jz += w * az;
-            kx += w * bx; ky += w * by; kz += w * bz;
+            const V W = PO::mk(w, w);
+            m0 = PO::fma(W, s0, m0);
+            mx = PO::fma(W, sx, mx);
+            my = PO::fma(W, sy, my);
+            mz = PO::fma(W, sz, mz);
         });
     } else {
-        unroll<13>([&](auto Kp) {
-            constexpr int i = dpair(decltype(Kp)::value);
-            constexpr int o = dopp(i);
-            constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
-            const R sf = f[i] + f[o], df = f[i] - f[o];
-            const R sg = g[i] + g[o], dg = g[i] - g[o];
-            rho += sf;
-            phi += sg;
-            if constexpr (cx == 1) { jx += df; kx += dg; }
-            if constexpr (cx == -1) { jx -= df; kx -= dg; }
-            if constexpr (cy == 1) { jy += df; ky += dg; }
-            if constexpr (cy == -1) { jy -= df; ky -= dg; }
-            if constexpr (cz == 1) { jz += df; kz += dg; }
-            if constexpr (cz == -1) { jz -= df; kz -= dg; }
-        });
+        unroll<13>([&](auto Kp) { pair_moments(Kp, m0, mx, my, mz); });
     }
+    const R rho = m0.x, phi = m0.y;
+    const R jx = mx.x, jy = my.x, jz = mz.x;
+    const R kx = mx.y, ky = my.y, kz = mz.y;
     if (!(fabs(rho) < (R)1e30) || !(fabs(phi) < (R)1e30)) atomicOr(&b.status->nonfinite, 1);
 
     const R fold = (R)fold_in;
@@ -266,69 +310,127 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     // scaled g at home: G* = g*/w - T_c = omc G + (g* - omc g)/w + (omc - 1) T_c - omc tlb c_ix
     const R gshift = SC ? (K.omc - (R)1) * Tc : (R)0;
     const R gtilt = SC ? -K.omc * K.tlb : (R)0;
+    const V OM = PO::mk(K.om, K.omc);
     {
         constexpr R w0 = (R)dweight(0);
         if constexpr (SC) {
-            f[0] = K.om * f[0] + (k0 - h * k1);
-            g[0] = K.omc * g[0] + ((ptb - pt * h) - pt * rho * (R)(1.0 / dweight(0)) + gshift);
+            fg[0] = PO::fma(OM, fg[0], PO::mk(k0 - h * k1, (ptb - pt * h) - pt * rho * (R)(1.0 / dweight(0)) + gshift));
         } else {
-            f[0] = K.om * f[0] + w0 * (k0 - h * k1);
-            g[0] = K.omc * g[0] + (w0 * (ptb - pt * h) - pt * rho);
+            fg[0] = PO::fma(OM, fg[0], PO::mk(w0 * (k0 - h * k1), w0 * (ptb - pt * h) - pt * rho));
         }
     }
     // Pairs grouped by weight class (face, edge, corner); the class constants fold w_i into the
-    // per-node coefficients and live only while their class is processed.
+    // per-node coefficients and live only while their class is processed.  Per direction pair
+    // (i, opp i):
+    //   S = (w (A k1 + k0) + w cx G B,  w pt (1 + rho + A))        the parts even in c
+    //   D = (w B k1 + w cx G (1 + A),   w pt B + w c.V)            the parts odd in c
+    //   (f*, g*)_i = (om, omc) (f, g)_i + S + D,  (f*, g*)_opp = (om, omc) (f, g)_opp + S - D.
     unroll<3>([&](auto C) {
         constexpr int c = decltype(C)::value + 1;
         // class weight; 1 in the scaled variables of shifted-FP16 storage (w_i divided out)
         constexpr R w = SC ? (R)1 : (R)(c == 1 ? 2.0 / 27.0 : (c == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
         const R wk1 = w * k1;
-        const R ca = (R)4.5 * wk1, cb = w * k0 - h * wk1, c3 = (R)3 * wk1;
         const R wG = w * G;
-        const R ce = (R)4.5 * wG, cd = wG - h * wG, cg = (R)3 * wG;
         const R wpt = w * pt;
-        const R ga = (R)4.5 * wpt, gc = (R)3 * wpt;
         R gb = w * ptb - h * wpt;
         if constexpr (SC) gb += gshift;
-        const R vx = w * Vx, vy = w * Vy, vz = w * Vz;
-        unroll<13>([&](auto Kp) {
-            constexpr int i = dpair(decltype(Kp)::value);
-            if constexpr (dclass(i) == c) {
-                constexpr int o = dopp(i);
-                constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
-                R cu = NZ, cV = NZ;
-                if constexpr (cx != 0) { cu += (R)cx * ux; cV += (R)cx * vx; }
-                if constexpr (cy != 0) { cu += (R)cy * uy; cV += (R)cy * vy; }
-                if constexpr (cz != 0) { cu += (R)cz * uz; cV += (R)cz * vz; }
-                const R q = cu * cu;
-                R wS = q * ca + cb;                 // w (A k1 + k0)
-                R wD = cu * c3;                     // w B k1
-                if constexpr (cx != 0) {
-                    wS += (R)cx * (cu * cg);        // w cx G B
-                    wD += (R)cx * (q * ce + cd);    // w cx G (1 + A)
+        if constexpr (sizeof(R) == 4 && !SC) {
+            // Packed: S and D as (f, g) pairs.  i is the member of the pair whose first nonzero
+            // component is +1 (S is even and D odd in c, so the choice is free), so the sums of
+            // the (u_k, u_k) and (., v_k) pairs start without a negation and the cx terms carry
+            // no sign.
+            const V UX = PO::mk(ux, ux), UY = PO::mk(uy, uy), UZ = PO::mk(uz, uz);
+            const V CA = PO::mk((R)4.5 * wk1, (R)4.5 * wpt);         // A coefficients
+            const V CB = PO::mk(w * k0 - h * wk1, gb);                // constant parts
+            const V C3 = PO::mk((R)3 * wk1, (R)3 * wpt);              // B coefficients
+            const V CE = PO::mk((R)4.5 * wG, (R)0);                   // f: cx G A
+            const V CG = PO::mk((R)3 * wG, (R)0);                     // f: cx G B
+            // (cx G (1 - 1.5 u^2), w c.V) from per-component pairs; the shifted-FP16 tilt
+            // -omc tlb c_ix rides on the x component of V
+            const V ZX = PO::mk(wG - h * wG, SC ? w * Vx + gtilt : w * Vx);
+            const V ZY = PO::mk(NZ, w * Vy), ZZ = PO::mk(NZ, w * Vz);
+            unroll<13>([&](auto Kp) {
+                constexpr int i0 = dpair(decltype(Kp)::value);
+                if constexpr (dclass(i0) == c) {
+                    constexpr int lead = dcx(i0) != 0 ? dcx(i0) : (dcy(i0) != 0 ? dcy(i0) : dcz(i0));
+                    constexpr int i = lead > 0 ? i0 : dopp(i0);
+                    constexpr int o = dopp(i);
+                    constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+                    // sum_k c_k P_k over the nonzero components, the first one +1
+                    auto csum = [&](const V &px, const V &py, const V &pz) {
+                        V r;
+                        if constexpr (cx != 0) r = px;
+                        else if constexpr (cy != 0) r = py;
+                        else r = pz;
+                        if constexpr (cx != 0 && cy == 1) r = PO::add(r, py);
+                        if constexpr (cx != 0 && cy == -1) r = PO::sub(r, py);
+                        if constexpr ((cx != 0 || cy != 0) && cz == 1) r = PO::add(r, pz);
+                        if constexpr ((cx != 0 || cy != 0) && cz == -1) r = PO::sub(r, pz);
+                        return r;
+                    };
+                    const V CU = csum(UX, UY, UZ);                     // (c.u, c.u)
+                    const V QQ = PO::mul(CU, CU);                      // ((c.u)^2, (c.u)^2)
+                    V Sv = PO::fma(QQ, CA, CB);
+                    V Z = csum(ZX, ZY, ZZ);
+                    if constexpr (cx != 0) {                           // cx = +1 here
+                        Sv = PO::fma(CU, CG, Sv);
+                        Z = PO::fma(QQ, CE, Z);
+                    }
+                    const V Dv = PO::fma(CU, C3, Z);
+                    fg[i] = PO::fma(OM, fg[i], PO::add(Sv, Dv));
+                    fg[o] = PO::fma(OM, fg[o], PO::sub(Sv, Dv));
                 }
-                const R gS = q * ga + gb;           // w pt (1 + rho + A)
-                R gD = cu * gc + cV;                // w pt B + w c.V
-                if constexpr (SC && cx != 0) gD += (R)cx * gtilt;
-                const R fi = f[i], fo = f[o], gi = g[i], go = g[o];
-                f[i] = K.om * fi + (wS + wD);
-                f[o] = K.om * fo + (wS - wD);
-                g[i] = K.omc * gi + (gS + gD);
-                g[o] = K.omc * go + (gS - gD);
-            }
-        });
+            });
+        } else {
+            // Scalar operations: FP64 (the pair form would spend FP64 instructions on its
+            // duplicated and zero lanes) and shifted FP16 (whose step, issue-bound at 96
+            // registers, ran 0.768 against 0.692 ms per odd step at 320x320x160 with the
+            // constant pairs)
+            const R ca = (R)4.5 * wk1, cb = w * k0 - h * wk1, c3 = (R)3 * wk1;
+            const R ce = (R)4.5 * wG, cd = wG - h * wG, cg = (R)3 * wG;
+            const R ga = (R)4.5 * wpt, gc = (R)3 * wpt;
+            const R vx = w * Vx, vy = w * Vy, vz = w * Vz;
+            unroll<13>([&](auto Kp) {
+                constexpr int i = dpair(decltype(Kp)::value);
+                if constexpr (dclass(i) == c) {
+                    constexpr int o = dopp(i);
+                    constexpr int cx = dcx(i), cy = dcy(i), cz = dcz(i);
+                    R cu = NZ, cV = NZ;
+                    if constexpr (cx != 0) { cu += (R)cx * ux; cV += (R)cx * vx; }
+                    if constexpr (cy != 0) { cu += (R)cy * uy; cV += (R)cy * vy; }
+                    if constexpr (cz != 0) { cu += (R)cz * uz; cV += (R)cz * vz; }
+                    const R q = cu * cu;
+                    R wS = q * ca + cb;                 // w (A k1 + k0)
+                    R wD = cu * c3;                     // w B k1
+                    if constexpr (cx != 0) {
+                        wS += (R)cx * (cu * cg);        // w cx G B
+                        wD += (R)cx * (q * ce + cd);    // w cx G (1 + A)
+                    }
+                    const R gS = q * ga + gb;           // w pt (1 + rho + A)
+                    R gD = cu * gc + cV;                // w pt B + w c.V
+                    if constexpr (SC && cx != 0) gD += (R)cx * gtilt;
+                    fg[i] = PO::fma(OM, fg[i], PO::mk(wS + wD, gS + gD));
+                    fg[o] = PO::fma(OM, fg[o], PO::mk(wS - wD, gS - gD));
+                }
+            });
+        }
     });
 
-    // store one slot: fv, gv in the working variables (shifted FP16: gv relative to T_c of the
-    // slot's own node)
-    auto put = [&](long long slot, R fv, R gv, double w) {
+    // the node index the scatter addresses from (an opaque copy with FRESH_SCATTER)
+    long long snode = node;
+    if constexpr (FRESH_SCATTER) asm("" : "+l"(snode));
+    S *const fS = fA + snode;
+    S *const gS = gA + snode;
+    // store the slot at offset rel from this node's slot of direction 0: (f, g) in the working
+    // variables (shifted FP16: g relative to T_c of the slot's own node)
+    auto put = [&](long long rel, const V &v, double w) {
         if constexpr (SC) {
-            fA[slot] = __floats2half2_rn(fv, gv);
+            fS[rel] = __float22half2_rn(v);
         } else if constexpr (ST::PAIRED) {
-            fA[slot] = make_float2(fv, gv);
+            fS[rel] = v;
         } else {
-            ST::st_f(fA + slot, fv, w, t0);
-            ST::st_g(gA + slot, gv, w, t0);
+            ST::st_f(fS + rel, v.x, w, t0);
+            ST::st_g(gS + rel, v.y, w, t0);
         }
     };
     auto scatter = [&](auto INT) {
@@ -339,7 +441,7 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
             constexpr double w = dweight(i);
             if constexpr (!ODD || i == 0) {
                 // even step: f*_i(x) swapped into the node's own slot (opp(i), x)
-                put((long long)o * L + node, f[i], g[i], w);
+                put((long long)o * L, fg[i], w);
             } else {
                 // odd step: f*_i(x) streams to slot (i, x + c_i); a population leaving the box
                 // becomes the next step's f_opp(i)(x) in slot (opp(i), x): bounce-back for f, and
@@ -350,11 +452,10 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
                     out = (cx == 1 && xhi) || (cx == -1 && xlo) || (cy == 1 && yhi) || (cy == -1 && ylo) ||
                           (cz == 1 && zhi) || (cz == -1 && zlo);
                 if (!out) {
-                    const long long off = (long long)cx + (long long)cy * geo.lx + (long long)cz * geo.lxy;
                     // shifted FP16: relative to T_c(x + c_i) = T_c(x) + tlb c_ix
-                    put((long long)i * L + node + off, f[i], SC ? g[i] - K.tlb * (R)cx : g[i], w);
+                    put(aa_gather(std::integral_constant<int, o>{}), SC && cx != 0 ? PO::mk(fg[i].x, fg[i].y - K.tlb * (R)cx) : fg[i], w);
                 } else {
-                    R gv = g[i];
+                    V v = fg[i];
                     if constexpr (cx != 0) {
                         const bool ox = (cx == 1) ? xhi : xlo;
                         const bool oyz = (cy == 1 && yhi) || (cy == -1 && ylo) || (cz == 1 && zhi) || (cz == -1 && zlo);
@@ -362,22 +463,22 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
                             const R tw = (cx == -1) ? K.thot : K.tcold;
                             if constexpr (SC) {
                                 const R wi = (R)w;
-                                gv = wall_image(wi * (g[i] + Tc), w, tw, rho) * (R)(1.0 / w) - Tc;
+                                v.y = wall_image(wi * (v.y + Tc), w, tw, rho) * (R)(1.0 / w) - Tc;
                             } else {
-                                gv = wall_image(g[i], w, tw, rho);
+                                v.y = wall_image(v.y, w, tw, rho);
                             }
                         }
                     }
-                    put((long long)o * L + node, f[i], gv, w);
+                    put((long long)o * L, v, w);
                 }
             }
             if constexpr (OUT == OUT_MACROS_COL) {
                 if constexpr (SC) {
-                    b.fcol[(long long)i * L + node] = (double)((R)w * f[i]);
-                    b.gcol[(long long)i * L + node] = (double)((R)w * (g[i] + Tc));
+                    b.fcol[(long long)i * L + node] = (double)((R)w * fg[i].x);
+                    b.gcol[(long long)i * L + node] = (double)((R)w * (fg[i].y + Tc));
                 } else {
-                    b.fcol[(long long)i * L + node] = (double)f[i];
-                    b.gcol[(long long)i * L + node] = (double)g[i];
+                    b.fcol[(long long)i * L + node] = (double)fg[i].x;
+                    b.gcol[(long long)i * L + node] = (double)fg[i].y;
                 }
             }
         });
