@@ -262,9 +262,9 @@ cudaError_t launch_step_mode(bool odd, int out, const Geo &geo, const Phys &ph,
 {
     // Warps of 32 x-nodes in one row (FP64, FP32: 16-wide blocks cost 3 % at 320x320x160, wider
     // ones nothing).  Shifted FP16 is issue-bound: its odd steps use 16 x 2 warps, so that half as
-    // many warps hold an x-face node and take the face-tested gather and scatter (0.717 against
-    // 0.729 ms for 32-wide blocks at 320x320x160); its even steps, which touch no neighbour, run
-    // best in 64-node rows (0.574 against 0.606 ms for 16 x 8 blocks).
+    // many warps hold an x-face node and take the face-tested gather and scatter (0.683 against
+    // 0.695 ms for 32-wide rows at 320x320x160); its even steps, which touch no neighbour, run
+    // best in 64-node rows (0.583 against 0.596 ms for 32-wide rows).
     dim3 blk(32, 4, 1);
     if (MODE == RBTP_STORE_F16S) blk = odd ? dim3(16, 8, 1) : (geo.lx % 64 == 0 ? dim3(64, 2, 1) : dim3(32, 4, 1));
     const dim3 grd = node_grid(geo, blk);

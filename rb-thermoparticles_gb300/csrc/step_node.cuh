@@ -61,19 +61,23 @@ struct PairOps<double> {
 // scatter to natural neighbour slots, walls at both ends); the even step reads and writes the
 // node's own slots only.  INTERIOR_PATH adds, for odd steps, a second copy of the gather and the
 // scatter without the box-face tests, taken by warps none of whose nodes touches a face.  It pays
-// only where the step is issue-bound (shifted-FP16 storage: -11 % instructions at 320x320x160);
-// FP32 is HBM-bound and FP64 FP64-pipe-bound, and the batched kernel (six step variants in one
-// kernel, small cavities whose warps nearly all touch an x face) leaves it out.
+// only where the step is issue-bound (shifted-FP16 storage: odd step 0.683 against 0.84 ms without
+// it at 320x320x160); FP32 is HBM-bound (measured the same with it) and FP64 FP64-pipe-bound, and
+// the batched kernel (six step variants in one kernel, small cavities whose warps nearly all touch
+// an x face) leaves it out.
 //
 // FRESH_SCATTER: the scatter addresses its slots from an opaque copy of the node index.  A node
 // writes exactly the slots it read (both parities), so otherwise the compiler keeps the gather's
-// addresses (two registers each) live across the collision rather than recompute them.  Where
-// the lattice sizes are per-thread values (the batched kernel stages them in shared memory) that
-// spilled 400-480 bytes per thread at 128 registers and the copy removes every spill (+7 % ensemble
-// throughput); with shifted FP16 it takes the odd step from 0.748 to 0.717 ms at 320x320x160.  FP32
-// gains nothing and FP64 (255 registers) loses half its speed, so they leave it out.
-template <int MODE, bool ODD, int OUT, bool INTERIOR_PATH = true, bool FRESH_SCATTER = MODE == RBTP_STORE_F16S && ODD,
-          bool HAS_OFF = true>
+// addresses (two registers each) live across the collision rather than recompute them.  The
+// batched kernel, whose lattice sizes are per-thread values (staged in shared memory), spills
+// 460-550 bytes per thread at 128 registers without it and none with it (+7 % ensemble
+// throughput).  The single-cavity kernel, addressing from its launch parameters, gains nothing
+// (FP32, shifted FP16) or loses half its speed (FP64), so it leaves it out.
+//
+// HAS_OFF: the odd-step slot offsets come from the launch's AAOff table (single-cavity kernel);
+// without it they are formed from the lattice sizes (batched kernel, one table per member would
+// cost shared memory for no gain).
+template <int MODE, bool ODD, int OUT, bool INTERIOR_PATH = true, bool FRESH_SCATTER = false, bool HAS_OFF = true>
 __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const StepBuffers &b, const AAOff &ao,
                                           int ix, int iy, int iz)
 {
