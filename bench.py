@@ -38,21 +38,31 @@ MEASURED_PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_step launch on the
-# 320x320x160 single-phase workload, from a one-pass ncu capture of
-# `python bench.py --only production:<storage> --steps 3 --warmup 3`
-# (the capture's summary is kept with the other ncu summaries).  Algorithmic bytes per launch: 16,384,000 nodes x
-# bytes_per_node.
-NCU_DRAM_BYTES = {"f64": 7.30e9 + 7.16e9, "f32": 3.62e9 + 3.63e9, "f16s": 1.84e9 + 1.80e9}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_step launch, the mean of one
+# even-step and one odd-step launch of the in-place storage, from one-pass ncu captures of
+# `python bench.py --only production:<storage> --steps 4 --warmup 3` (FP32, shifted FP16: the
+# 320x320x160 workload itself) and `... --only production:f64 --grid 192x192x96 ...` (FP64, 3.1 GB
+# per launch, scaled to 16,384,000 nodes by the node count; its reads are exactly 440 B per node,
+# its writes 423 B per node because L2 still holds part of them when the kernel ends).  The
+# captures' summary is kept with the other ncu summaries.  Algorithmic bytes per launch:
+# 16,384,000 nodes x bytes_per_node.
+NCU_DRAM_BYTES = {
+    "f32": ((3.607174144e9 + 3.569068288e9) + (3.604580352e9 + 3.557273600e9)) / 2,
+    "f16s": ((1.835989248e9 + 1.781190144e9) + (1.835062016e9 + 1.772242432e9)) / 2,
+    "f64": ((1.558169344e9 + 1.497404672e9) + (1.557334528e9 + 1.492732416e9)) / 2 * 16384000 / (192 * 192 * 96),
+}
 
 
-# FP64 work of one FP64 k_step node update, from one ncu capture of k_step<0,1,0> on 128x128x64
-# (1,048,576 nodes) with `python bench.py --only production:f64 --grid 128x128x64 --steps 3
-# --warmup 3`: smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum = 187,981,633 /
-# 206,585,856 / 66,158,592 instructions, i.e. per node 179.3 DFMA + 197.0 DADD + 63.1 DMUL =
-# 439.4 FP64 arithmetic instructions and 618.7 flops (an FMA counts 2).
-FP64_FLOPS_PER_NODE = (2 * 187981633 + 206585856 + 66158592) / 1048576
-FP64_INST_PER_NODE = (187981633 + 206585856 + 66158592) / 1048576
+# FP64 work of one FP64 k_step node update, from one ncu capture of an odd and an even launch
+# (k_step<0,1,0>, k_step<0,0,0>) on 128x128x64 (1,048,576 nodes) with `python bench.py --only
+# production:f64 --grid 128x128x64 --steps 4 --warmup 3`:
+# smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum per node, odd / even:
+# 167.41 / 167.00 DFMA, 189.15 / 189.00 DADD, 68.23 / 68.00 DMUL, i.e. 424.4 FP64 arithmetic
+# instructions (426.4 with the FP64 compares and conversions) and 591.6 flops (an FMA counts 2)
+# per node on average.
+_FP64_DFMA, _FP64_DADD, _FP64_DMUL = (167.41 + 167.00) / 2, (189.15 + 189.00) / 2, (68.23 + 68.00) / 2
+FP64_FLOPS_PER_NODE = 2 * _FP64_DFMA + _FP64_DADD + _FP64_DMUL
+FP64_INST_PER_NODE = _FP64_DFMA + _FP64_DADD + _FP64_DMUL
 
 
 def bytes_per_node(storage: int) -> int:
@@ -608,7 +618,7 @@ def run_ours(args) -> dict:
         "config": {"workload": "production single-phase RB 320x320x160, Ra=1e8, Pr=0.71, FP32-store",
                    "arithmetic": "FP32 population storage and FP32 step arithmetic (FP64 reductions)",
                    "nodes": head["nodes"], "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
-                   "l2": "state (7.2 GB) exceeds L2; no flush needed"},
+                   "l2": "state (3.5 GB of populations, in place) exceeds L2; no flush needed"},
         "roofline": head["roofline"],
         "clocks": clocks,
         "gpu_launches": head["launches_per_step"] * args.steps,
