@@ -10,11 +10,12 @@ restatement of the reference step, pinned against the reference's kernels elsewh
    in seconds.  Recorded: the density deviation passes -0.5 (half the rest density) at step 3,
    the spheres stay in the box through step 11 and leave it at step 12.  At density ratio 1.0
    (no particle buoyancy) the same case stays near rest.
-2. Two requests of the serving benchmark's mix, both 32x32x16 cavities (g0 = 10 lattice units)
+2. Three requests of the serving benchmark's mix, all 32x32x16 cavities (g0 = 10 lattice units)
    holding 137-143 spheres of diameter 3.2 (about 15 % solid): request 14 (Ra = 2.9e7, relaxation
-   time 0.505) and request 7 (Ra = 7.9e5, 0.525).  Spheres leave the box at step 2889 (request
-   14) and step 18183 (request 7), within the requests' horizons; the density deviation exceeds
-   0.5 in magnitude long before.  The CUDA path reports RBTP_ERR_NONFINITE for them.  Request 7 takes
+   time 0.505), request 8 (Ra = 5.7e6, 0.511) and request 7 (Ra = 7.9e5, 0.525).  Spheres leave the
+   box at step 2889 (request 14), step 2692 (request 8, density deviation beyond 0.5 from step 929)
+   and step 18183 (request 7), within the requests' horizons; the density deviation exceeds 0.5 in
+   magnitude long before.  The CUDA path reports RBTP_ERR_NONFINITE for them.  Request 7 takes
    about three minutes of oracle time and runs with RBTP_SLOW_TESTS=1.
 """
 import math
@@ -86,6 +87,7 @@ def _serving_request(k):
 
 @pytest.mark.parametrize("k,escape_step", [
     (14, 2889),
+    (8, 2692),
     pytest.param(7, 18183, marks=pytest.mark.skipif(not os.environ.get("RBTP_SLOW_TESTS"),
                                                     reason="three minutes of oracle time; RBTP_SLOW_TESTS=1")),
 ])
