@@ -171,6 +171,7 @@ int refresh(rbtp_batch *b)
         std::memset(&d, 0, sizeof(d));
         d.geo = h->geo;
         d.ph = h->ph;
+        d.aoff = make_aa_off(h->geo);
         d.f = h->f;
         d.g = h->g;
         for (int k = 0; k < 2; ++k) d.owner[k] = h->owner[k];

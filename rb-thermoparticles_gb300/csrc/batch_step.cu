@@ -55,17 +55,19 @@ __global__ void k_batch_advance(CavDesc *desc, int n)
 }
 
 template <int MODE, bool ODD>
-__device__ __forceinline__ void step_out(const Geo &geo, const Phys &ph, const StepBuffers &b, int out, int ix,
-                                         int iy, int iz)
+__device__ __forceinline__ void step_out(const Geo &geo, const Phys &ph, const AAOff &ao, const StepBuffers &b,
+                                         int out, int ix, int iy, int iz)
 {
-    if (out == OUT_NONE) step_node<MODE, ODD, OUT_NONE, false, MODE != RBTP_STORE_F64, false>(geo, ph, b, AAOff{}, ix, iy, iz);
-    else if (out == OUT_RHO) step_node<MODE, ODD, OUT_RHO, false, MODE != RBTP_STORE_F64, false>(geo, ph, b, AAOff{}, ix, iy, iz);
-    else step_node<MODE, ODD, OUT_MACROS, false, MODE != RBTP_STORE_F64, false>(geo, ph, b, AAOff{}, ix, iy, iz);
+    if (out == OUT_NONE) step_node<MODE, ODD, OUT_NONE, false, MODE != RBTP_STORE_F64, true, true>(geo, ph, b, ao, ix, iy, iz);
+    else if (out == OUT_RHO) step_node<MODE, ODD, OUT_RHO, false, MODE != RBTP_STORE_F64, true, true>(geo, ph, b, ao, ix, iy, iz);
+    else step_node<MODE, ODD, OUT_MACROS, false, MODE != RBTP_STORE_F64, true, true>(geo, ph, b, ao, ix, iy, iz);
 }
 
 // The batched kernel carries all phase/output variants of the step body behind block-uniform
 // branches; it is given more registers than the single-cavity kernel (4 resident blocks of 128)
-// to keep them in registers.
+// to keep them in registers.  Its step body takes the scatter index from an opaque copy
+// (FRESH_SCATTER), the odd-step offsets from the member's AAOff staged in shared memory, and the
+// face tests from per-node masks (FACE_MASK); see step_node.cuh for what each is worth.
 #ifndef RBTP_BATCH_MINB_LOW
 #define RBTP_BATCH_MINB_LOW 4
 #endif
@@ -80,15 +82,17 @@ __global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MI
     // reads them many times; the single-cavity kernel has them as launch parameters)
     __shared__ Geo sgeo;
     __shared__ Phys sph;
-    constexpr int GW = sizeof(Geo) / 4, PW = sizeof(Phys) / 4;
+    __shared__ AAOff soff;
+    constexpr int GW = sizeof(Geo) / 4, PW = sizeof(Phys) / 4, OW = sizeof(AAOff) / 4;
     const int tid = threadIdx.y * TX + threadIdx.x;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int4 tl = tiles[t];
         const CavDesc &d = desc[tl.x];
         __syncthreads();   // the previous tile's readers are done
-        for (int k = tid; k < GW + PW; k += TX * TY) {
+        for (int k = tid; k < GW + PW + OW; k += TX * TY) {
             if (k < GW) reinterpret_cast<int *>(&sgeo)[k] = reinterpret_cast<const int *>(&d.geo)[k];
-            else reinterpret_cast<int *>(&sph)[k - GW] = reinterpret_cast<const int *>(&d.ph)[k - GW];
+            else if (k < GW + PW) reinterpret_cast<int *>(&sph)[k - GW] = reinterpret_cast<const int *>(&d.ph)[k - GW];
+            else reinterpret_cast<int *>(&soff)[k - GW - PW] = reinterpret_cast<const int *>(&d.aoff)[k - GW - PW];
         }
         __syncthreads();
         const int ix = tl.y * TX + threadIdx.x, iy = tl.z * TY + threadIdx.y, iz = tl.w;
@@ -101,8 +105,8 @@ __global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MI
         b.rho = d.rho; b.ux = d.ux; b.uy = d.uy; b.uz = d.uz; b.phi = d.phi;
         b.fcol = nullptr; b.gcol = nullptr;
         b.status = d.status;
-        if (d.phase == PHASE_SWAPPED) step_out<MODE, true>(sgeo, sph, b, d.out, ix, iy, iz);
-        else step_out<MODE, false>(sgeo, sph, b, d.out, ix, iy, iz);
+        if (d.phase == PHASE_SWAPPED) step_out<MODE, true>(sgeo, sph, soff, b, d.out, ix, iy, iz);
+        else step_out<MODE, false>(sgeo, sph, soff, b, d.out, ix, iy, iz);
     }
 }
 

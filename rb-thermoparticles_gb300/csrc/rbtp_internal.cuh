@@ -426,6 +426,7 @@ cudaError_t launch_refill(int mode, const Geo &geo, const Phys &ph, const PartBu
 struct CavDesc {
     Geo geo;
     Phys ph;
+    AAOff aoff;                         // odd-step slot offsets of this member's lattice
     void *f, *g;                        // the population array (in-place AA storage)
     void *faux;                         // F_x auxiliary (Store<MODE>::A)
     double *rho_wall, *rho, *ux, *uy, *uz, *phi;
