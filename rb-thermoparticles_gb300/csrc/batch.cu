@@ -106,7 +106,7 @@ int rebuild(rbtp_batch *b)
         for (int m = 0; m < n; ++m) {
             const Geo &g = b->members[m]->geo;
             const int nx = (g.lx + tx[s] - 1) / tx[s], ny = (g.ly + ty[s] - 1) / ty[s];
-            for (int z = 0; z < g.lz; ++z)
+            for (int z = 0; z < g.lz; z += BATCH_TILE_Z)
                 for (int y = 0; y < ny; ++y)
                     for (int x = 0; x < nx; ++x) t.push_back(make_int4(m, x, y, z));
         }

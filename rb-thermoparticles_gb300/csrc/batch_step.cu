@@ -95,7 +95,8 @@ __global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MI
             else reinterpret_cast<int *>(&soff)[k - GW - PW] = reinterpret_cast<const int *>(&d.aoff)[k - GW - PW];
         }
         __syncthreads();
-        const int ix = tl.y * TX + threadIdx.x, iy = tl.z * TY + threadIdx.y, iz = tl.w;
+        // tile (member, x, y, z0): BATCH_TILE_Z planes from z0
+        const int ix = tl.y * TX + threadIdx.x, iy = tl.z * TY + threadIdx.y, z0 = tl.w;
         if (d.out == OUT_IDLE || ix >= sgeo.lx || iy >= sgeo.ly) continue;
         StepBuffers b;
         b.f = d.f;
@@ -105,8 +106,12 @@ __global__ void __launch_bounds__(TX * TY, MODE == RBTP_STORE_F64 ? RBTP_STEP_MI
         b.rho = d.rho; b.ux = d.ux; b.uy = d.uy; b.uz = d.uz; b.phi = d.phi;
         b.fcol = nullptr; b.gcol = nullptr;
         b.status = d.status;
-        if (d.phase == PHASE_SWAPPED) step_out<MODE, true>(sgeo, sph, soff, b, d.out, ix, iy, iz);
-        else step_out<MODE, false>(sgeo, sph, soff, b, d.out, ix, iy, iz);
+        const int z1 = min(z0 + BATCH_TILE_Z, sgeo.lz);
+        if (d.phase == PHASE_SWAPPED) {
+            for (int iz = z0; iz < z1; ++iz) step_out<MODE, true>(sgeo, sph, soff, b, d.out, ix, iy, iz);
+        } else {
+            for (int iz = z0; iz < z1; ++iz) step_out<MODE, false>(sgeo, sph, soff, b, d.out, ix, iy, iz);
+        }
     }
 }
 

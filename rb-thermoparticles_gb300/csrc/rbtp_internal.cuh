@@ -449,6 +449,12 @@ struct CavDesc {
 };
 
 constexpr int BATCH_SHAPES = 2;  // tile shapes of the batched step: 0 = 32x4, 1 = 64x2
+// z-planes per tile of the batched step: a block stages its member's constants once and steps
+// BATCH_TILE_Z planes of its (x, y) tile
+#ifndef RBTP_BATCH_TILE_Z
+#define RBTP_BATCH_TILE_Z 4
+#endif
+constexpr int BATCH_TILE_Z = RBTP_BATCH_TILE_Z;
 cudaError_t launch_batch_plan(CavDesc *desc, int n, cudaStream_t st);
 cudaError_t launch_batch_advance(CavDesc *desc, int n, cudaStream_t st);
 cudaError_t launch_step_batched(int mode, int shape, const CavDesc *desc, const int4 *tiles,
