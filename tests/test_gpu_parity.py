@@ -100,7 +100,7 @@ def test_reduced_storage_against_fp64(env, storage, tol_phi, tol_u, tol_nu):
     f, g, f7 = W.initial_state(cfg)
     s.load_state(f, g, f7)
     o.load_state(f, g, f7)
-    # the first step after a load collides home slots (no pull)
+    # the first step after a load is an even step: it collides the natural slots (no gather)
     s.step(1, macros_last=True)
     o.step(1)
     assert rel_l2(s.macros()["phi"], o.macros()["phi"]) < 1e-6
