@@ -655,7 +655,10 @@ int rbtp_step_ex(rbtp_handle *h, int nsteps, unsigned flags)
             // Stream order: the contacts (positions only) run on the side stream beside IBB (both
             // latency-bound, few CTAs); the integrator waits for the contact forces.  The link
             // slabs stay on the main stream: beside the HBM-bound bulk kernel their CTAs would take
-            // its SM slots (measured slower).
+            // its SM slots (measured slower).  The particle kernels use ordinary launches:
+            // programmatic dependent launch, which lets each one's blocks become resident while
+            // its predecessor finishes, made the 1000-sphere step 0.3 % (FP32) and 0.6 % (FP64)
+            // slower.
             int *oc = h->owner[h->ocur], *on = h->owner[1 - h->ocur];
             CK(cudaEventRecord(h->ev_fork, h->stream));
             CK(cudaStreamWaitEvent(h->side, h->ev_fork, 0));
