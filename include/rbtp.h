@@ -216,7 +216,7 @@ int  rbtp_write_particles(rbtp_handle *h, const char *dir, int istep);   /* outp
 int  rbtp_checkpoint_write(rbtp_handle *h, const char *path);
 int  rbtp_checkpoint_read(rbtp_handle *h, const char *path);
 
-/* ---- batched execution (spec addition: many cavities, one persistent launch) ---------- */
+/* ---- batched execution (beyond the reference: many cavities, one persistent launch) -------- */
 /* A batch advances many independent cavities (own sizes, Ra, Pr, particle counts; one storage
  * mode) in lockstep: per step ONE persistent launch of the fused step over a packed tile table of all
  * cavities, one launch per particle kernel for all spheres of all cavities, the whole step captured
@@ -263,7 +263,7 @@ int  rbtp_batch_set_launch(rbtp_batch *b, int shape, int grid);
 /* Device bytes rbtp_create allocates for cfg (the admission currency of the server below). */
 int  rbtp_footprint(const rbtp_config *cfg, size_t *bytes);
 
-/* ---- continuous-batching solve server (spec addition) ------------------------------------ */
+/* ---- continuous-batching solve server (beyond the reference) ----------------------------------- */
 /* Requests (case, horizon in steps, Nu sampling cadence) are queued from any thread.  Each tick
  * launches max_steps steps of the batch of active requests (bounded by the longest remaining
  * horizon and the sample-ring capacity; each request stops on the device at its own horizon and

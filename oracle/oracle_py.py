@@ -1,7 +1,8 @@
 """ctypes wrapper of the CPU oracle (oracle/rbtp_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
-leg as the checker.  The product library never imports it.  The interface mirrors rbtp.Solver so
+leg, as the reference against which the library is compared.  The product library never imports
+it.  The interface mirrors rbtp.Solver so
 that parity tests read the same on both sides.
 """
 from __future__ import annotations

@@ -88,7 +88,7 @@ def test_reference_pin_config1_100_and_1000_steps(ref_driver, oracle_mod, tmp_pa
     fr, gr = np.fromfile(out1000 / "f.bin"), np.fromfile(out1000 / "g.bin")
     mr = np.fromfile(out1000 / "macros.bin").reshape(6, L)
     err = max(rel_l2(gs, gr), np.linalg.norm(fs - fr) / np.linalg.norm(gr))
-    print(f"config 1 after 1000 steps: relative L2 {err:.3e}")
+    print(f"64x64x32 Ra=1e6 after 1000 steps: relative L2 {err:.3e}")
     _fields_close(fs, gs, fr, gr)
     _macros_close(s.macros(), mr)
 
