@@ -74,9 +74,9 @@ struct PairOps<double> {
 // node's own slots only.  INTERIOR_PATH adds, for odd steps, a second copy of the gather and the
 // scatter without the box-face tests, taken by warps none of whose nodes touches a face.  It pays
 // only where the step is issue-bound (shifted-FP16 storage: odd step 0.683 against 0.84 ms without
-// it at 320x320x160); FP32 is HBM-bound (measured the same with it) and FP64 FP64-pipe-bound, and
-// the batched kernel (six step variants in one kernel, small cavities whose warps nearly all touch
-// an x face) leaves it out.
+// it at 320x320x160); FP32 is HBM-bound (measured the same with it), FP64 FP64-pipe-bound, and
+// the batched kernel (six step variants in one kernel at 128 registers) ran 0.7 % slower with it
+// (9,010 against 9,073 MLUPS for the 256-cavity ensemble), so they leave it out.
 //
 // FRESH_SCATTER: the scatter addresses its slots from an opaque copy of the node index.  A node
 // writes exactly the slots it read (both parities), so otherwise the compiler keeps the gather's
@@ -95,8 +95,8 @@ struct PairOps<double> {
 // 320x320x160: FP64 odd step 13.24 against 13.41 ms, batched ensemble +0.5 % (with the staged
 // offset table); the single-cavity FP32 and shifted-FP16 odd steps run 1-2 % slower with it, so
 // they keep the flag expressions.
-template <int MODE, bool ODD, int OUT, bool INTERIOR_PATH = true, bool FRESH_SCATTER = false, bool HAS_OFF = true,
-          bool FACE_MASK = MODE == RBTP_STORE_F64>
+template <int MODE, bool ODD, int OUT, bool INTERIOR_PATH = MODE == RBTP_STORE_F16S, bool FRESH_SCATTER = false,
+          bool HAS_OFF = true, bool FACE_MASK = MODE == RBTP_STORE_F64>
 __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const StepBuffers &b, const AAOff &ao,
                                           int ix, int iy, int iz)
 {
@@ -200,7 +200,7 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
         });
     };
     const bool face = xlo || xhi || ylo || yhi || zlo || zhi;
-    const bool interior = INTERIOR_PATH && SC && ODD && !__any_sync(__activemask(), face);
+    const bool interior = INTERIOR_PATH && ODD && !__any_sync(__activemask(), face);
     if (interior) gather(std::true_type{});
     else gather(std::false_type{});
     if constexpr (!ODD && SC) {
