@@ -58,9 +58,9 @@ template <int MODE, bool ODD>
 __device__ __forceinline__ void step_out(const Geo &geo, const Phys &ph, const AAOff &ao, const StepBuffers &b,
                                          int out, int ix, int iy, int iz)
 {
-    if (out == OUT_NONE) step_node<MODE, ODD, OUT_NONE, false, MODE != RBTP_STORE_F64, true, true>(geo, ph, b, ao, ix, iy, iz);
-    else if (out == OUT_RHO) step_node<MODE, ODD, OUT_RHO, false, MODE != RBTP_STORE_F64, true, true>(geo, ph, b, ao, ix, iy, iz);
-    else step_node<MODE, ODD, OUT_MACROS, false, MODE != RBTP_STORE_F64, true, true>(geo, ph, b, ao, ix, iy, iz);
+    if (out == OUT_NONE) step_node<MODE, ODD, OUT_NONE, false, MODE != RBTP_STORE_F64, true>(geo, ph, b, ao, ix, iy, iz);
+    else if (out == OUT_RHO) step_node<MODE, ODD, OUT_RHO, false, MODE != RBTP_STORE_F64, true>(geo, ph, b, ao, ix, iy, iz);
+    else step_node<MODE, ODD, OUT_MACROS, false, MODE != RBTP_STORE_F64, true>(geo, ph, b, ao, ix, iy, iz);
 }
 
 // The batched kernel carries all phase/output variants of the step body behind block-uniform

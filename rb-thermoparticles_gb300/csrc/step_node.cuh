@@ -86,9 +86,8 @@ struct PairOps<double> {
 // throughput).  The single-cavity kernel, addressing from its launch parameters, gains nothing
 // (FP32, shifted FP16) or loses half its speed (FP64), so it leaves it out.
 //
-// HAS_OFF: the odd-step slot offsets come from an AAOff table (the launch parameters of the
-// single-cavity kernel, a copy staged in shared memory per member in the batched kernel); without
-// it they are formed from the lattice sizes.
+// The odd-step slot offsets come from an AAOff table: the launch parameters of the single-cavity
+// kernel, a copy staged in shared memory per member in the batched kernel.
 //
 // FACE_MASK: the per-direction box-face tests read bits of two per-node masks built once from the
 // six face flags, instead of evaluating the flags' disjunction per direction.  Measured at
@@ -96,7 +95,7 @@ struct PairOps<double> {
 // offset table); the single-cavity FP32 and shifted-FP16 odd steps run 1-2 % slower with it, so
 // they keep the flag expressions.
 template <int MODE, bool ODD, int OUT, bool INTERIOR_PATH = MODE == RBTP_STORE_F16S, bool FRESH_SCATTER = false,
-          bool HAS_OFF = true, bool FACE_MASK = MODE == RBTP_STORE_F64>
+          bool FACE_MASK = MODE == RBTP_STORE_F64>
 __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const StepBuffers &b, const AAOff &ao,
                                           int ix, int iy, int iz)
 {
@@ -115,16 +114,8 @@ __device__ __forceinline__ void step_node(const Geo &geo, const Phys &ph, const 
     // 1.6-2x the even steps' instructions).
     const S *const fN = fA + node;
     const S *const gN = gA + node;
-    // the odd step's gather offset of direction I (AAOff): from the launch parameters, or formed
-    // from the lattice sizes where the caller has no table (the batched kernel)
-    auto aa_gather = [&](auto I) -> long long {
-        constexpr int i = decltype(I)::value;
-        if constexpr (HAS_OFF) {
-            return ao.g[i];
-        } else {
-            return (long long)dopp(i) * L - ((long long)dcx(i) + (long long)dcy(i) * geo.lx + (long long)dcz(i) * geo.lxy);
-        }
-    };
+    // the odd step's gather offset of direction I (AAOff)
+    auto aa_gather = [&](auto I) -> long long { return ao.g[decltype(I)::value]; };
     const double t0 = ph.t0;
     const bool xlo = ix == 0, xhi = ix == geo.lx - 1;
     const bool ylo = iy == 0, yhi = iy == geo.ly - 1;
